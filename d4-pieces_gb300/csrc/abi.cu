@@ -1,0 +1,397 @@
+// abi.cu -- extern "C" boundary (include/d4e.h) over the engine.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/d4e.h"
+#include "engine.h"
+#include "kernels.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+template <class F>
+int guarded(F &&f) {
+    try {
+        g_err.clear();
+        return f();
+    } catch (const d4e::Error &e) {
+        return fail(e.code, e.what());
+    } catch (const std::bad_alloc &) {
+        return fail(D4E_ERR_NOMEM, "host allocation failed");
+    } catch (const std::exception &e) {
+        return fail(D4E_ERR_INVALID, e.what());
+    }
+}
+
+}  // namespace
+
+struct d4e_frow {
+    std::vector<uint64_t> shapes;
+    std::vector<uint32_t> counts;
+    uint32_t sym = 0xFF;
+    uint32_t width = 8;
+    d4e::PieceLib lib;
+    int device = -1;
+};
+
+struct d4e_searcher {
+    std::unique_ptr<d4e::Engine> eng;
+    uint32_t id = 0;
+    uint32_t width = 8, height = 0;
+    std::vector<uint8_t> rows;
+};
+
+extern "C" {
+
+const char *d4e_last_error(void) { return g_err.c_str(); }
+
+const char *d4e_version(void) { return "d4e 0.1 (sm_103a)"; }
+
+int d4e_device_count(int32_t *n) {
+    return guarded([&] {
+        if (!n)
+            return fail(D4E_ERR_INVALID, "null pointer");
+        int c = 0;
+        if (cudaGetDeviceCount(&c) != cudaSuccess) {
+            cudaGetLastError();
+            c = 0;
+        }
+        *n = c;
+        return D4E_OK;
+    });
+}
+
+int d4e_show_gpu_devices(void) {
+    return guarded([&] {
+        int n = 0;
+        d4e::cuda_check(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+        std::printf("Number of devices: %d\n", n);
+        for (int i = 0; i < n; i++) {
+            cudaDeviceProp p;
+            d4e::cuda_check(cudaGetDeviceProperties(&p, i), "cudaGetDeviceProperties");
+            std::printf("Device Number: %d\n", i);
+            std::printf("  Device name: %s\n", p.name);
+            std::printf("  Capability: %d.%d\n", p.major, p.minor);
+            std::printf("  MP: %d\n", p.multiProcessorCount);
+            std::printf("  Memory Bus Width (bits): %d\n", p.memoryBusWidth);
+            std::printf("  Global mem (MiB): %.1f\n", p.totalGlobalMem / 1048576.0);
+            std::printf("  L2 Cache Size (B): %d\n", p.l2CacheSize);
+            std::printf("  Shared mem per block optin (B): %zu\n", p.sharedMemPerBlockOptin);
+            std::printf("  Shared mem per mp (B): %zu\n", p.sharedMemPerMultiprocessor);
+            std::printf("  Threads/mp: %d\n", p.maxThreadsPerMultiProcessor);
+            std::printf("  Registers per mp: %d\n", p.regsPerMultiprocessor);
+        }
+        return D4E_OK;
+    });
+}
+
+int d4e_catalogue(uint32_t m, int32_t onesided, uint64_t *out, uint32_t max, uint32_t *n) {
+    return guarded([&] {
+        if (m < 1 || m > 8)
+            return fail(D4E_ERR_INVALID, "catalogue covers 1..8 cells");
+        const auto &v = onesided ? d4e::catalogue_onesided((int)m) : d4e::catalogue_free((int)m);
+        if (n)
+            *n = (uint32_t)v.size();
+        for (uint32_t i = 0; out && i < max && i < v.size(); i++)
+            out[i] = v[i];
+        return D4E_OK;
+    });
+}
+
+int d4e_frow_create(const uint64_t *shapes, const uint32_t *counts, uint32_t n_pieces,
+                    uint32_t sym, uint32_t width, int32_t show_report, d4e_frow **out) {
+    return guarded([&] {
+        if (!out || (n_pieces && (!shapes || !counts)))
+            return fail(D4E_ERR_INVALID, "null pointer");
+        auto f = std::make_unique<d4e_frow>();
+        f->shapes.assign(shapes, shapes + n_pieces);
+        f->counts.assign(counts, counts + n_pieces);
+        f->sym = sym;
+        f->width = width;
+        const std::string err = d4e::build_piece_lib(shapes, counts, n_pieces, sym, width, f->lib);
+        if (!err.empty())
+            return fail(err.find("more than") != std::string::npos ? D4E_ERR_UNSUPPORTED
+                                                                   : D4E_ERR_INVALID,
+                        err);
+        if (show_report) {
+            for (uint32_t c = 0; c < width; c++)
+                std::printf("[col %u] => %u placements\n", c, (unsigned)f->lib.col_len[c]);
+        }
+        *out = f.release();
+        return D4E_OK;
+    });
+}
+
+int d4e_frow_transfer(d4e_frow *f, int32_t device) {
+    return guarded([&] {
+        if (!f)
+            return fail(D4E_ERR_INVALID, "null frow");
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+            cudaGetLastError();
+            return fail(D4E_ERR_CUDA, "no CUDA device");
+        }
+        if (device < 0 || device >= n)
+            return fail(D4E_ERR_INVALID, "no such CUDA device");
+        f->device = device;
+        return D4E_OK;
+    });
+}
+
+int d4e_frow_placements(const d4e_frow *f, uint32_t col, uint32_t *n) {
+    return guarded([&] {
+        if (!f || !n)
+            return fail(D4E_ERR_INVALID, "null pointer");
+        if (col >= f->width)
+            return fail(D4E_ERR_INVALID, "column out of range");
+        *n = f->lib.col_len[col];
+        return D4E_OK;
+    });
+}
+
+void d4e_frow_destroy(d4e_frow *f) { delete f; }
+
+static int make_searcher(const d4e_frow *f, uint32_t height, const uint8_t *rows, uint32_t flags,
+                         d4e_searcher **out) {
+    if (!f || !out || !rows)
+        return fail(D4E_ERR_INVALID, "null pointer");
+    if (f->device < 0)
+        return fail(D4E_ERR_STATE, "frow tables not transferred to a device");
+    auto s = std::make_unique<d4e_searcher>();
+    d4e::EngineOpts o;
+    o.device = f->device;
+    o.keep_levels = (flags & D4E_KEEP_LEVELS) != 0;
+    s->eng = std::make_unique<d4e::Engine>(o);
+    d4e::InstanceSpec sp;
+    sp.width = f->width;
+    sp.height = height;
+    sp.rows = rows;
+    sp.shapes = f->shapes.data();
+    sp.counts = f->counts.data();
+    sp.n_pieces = (uint32_t)f->shapes.size();
+    sp.sym = f->sym;
+    s->id = s->eng->add(sp);
+    s->width = f->width;
+    s->height = height;
+    s->rows.assign(rows, rows + height);
+    *out = s.release();
+    return D4E_OK;
+}
+
+int d4e_searcher_create(const d4e_frow *f, uint64_t empty_area, d4e_searcher **out) {
+    return guarded([&] {
+        if (!f)
+            return fail(D4E_ERR_INVALID, "null frow");
+        if (f->width != 8)
+            return fail(D4E_ERR_INVALID, "empty_area boards are 8 wide");
+        // height = ceil(bit_width(empty_area) / 8), src/searcher_cuda.cu:13
+        uint32_t bw = 0;
+        for (uint64_t v = empty_area; v; v >>= 1)
+            bw++;
+        const uint32_t h = (bw + 7) / 8;
+        if (h == 0)
+            return fail(D4E_ERR_INVALID, "empty board");
+        uint8_t rows[8];
+        for (uint32_t r = 0; r < 8; r++)
+            rows[r] = (uint8_t)(empty_area >> (8 * r));
+        return make_searcher(f, h, rows, 0, out);
+    });
+}
+
+int d4e_searcher_create_board(const d4e_frow *f, uint32_t height, const uint8_t *rows,
+                              uint32_t flags, d4e_searcher **out) {
+    return guarded([&] { return make_searcher(f, height, rows, flags, out); });
+}
+
+int d4e_searcher_get_height(const d4e_searcher *s, uint32_t *height) {
+    return guarded([&] {
+        if (!s || !height)
+            return fail(D4E_ERR_INVALID, "null pointer");
+        *height = s->height - s->eng->row(s->id);
+        if (s->eng->done(s->id))
+            *height = 0;
+        return D4E_OK;
+    });
+}
+
+int d4e_searcher_size(const d4e_searcher *s, uint64_t *n) {
+    return guarded([&] {
+        if (!s || !n)
+            return fail(D4E_ERR_INVALID, "null pointer");
+        *n = s->eng->done(s->id) ? 0 : std::max<uint64_t>(s->eng->frontier_size(s->id), 1);
+        return D4E_OK;
+    });
+}
+
+int d4e_searcher_bucket_size(d4e_searcher *s, uint32_t bucket, uint64_t *n) {
+    return guarded([&] {
+        if (!s || !n)
+            return fail(D4E_ERR_INVALID, "null pointer");
+        if (bucket > 255)
+            return fail(D4E_ERR_INVALID, "bucket is an 8-bit row pattern");
+        *n = s->eng->bucket_count(s->id, bucket);
+        return D4E_OK;
+    });
+}
+
+int d4e_searcher_next_size(const d4e_searcher *s, uint64_t *n) {
+    return guarded([&] {
+        if (!s || !n)
+            return fail(D4E_ERR_INVALID, "null pointer");
+        *n = s->eng->next_size_estimate(s->id);
+        return D4E_OK;
+    });
+}
+
+int d4e_searcher_search_GPU(d4e_searcher *s) {
+    return guarded([&] {
+        if (!s)
+            return fail(D4E_ERR_INVALID, "null searcher");
+        if (s->eng->done(s->id))
+            return fail(D4E_ERR_STATE, "height is already 0");
+        s->eng->step();
+        return D4E_OK;
+    });
+}
+
+int d4e_searcher_run(d4e_searcher *s) {
+    return guarded([&] {
+        if (!s)
+            return fail(D4E_ERR_INVALID, "null searcher");
+        s->eng->run();
+        return D4E_OK;
+    });
+}
+
+int d4e_searcher_count(d4e_searcher *s, uint64_t *count) {
+    return guarded([&] {
+        if (!s || !count)
+            return fail(D4E_ERR_INVALID, "null pointer");
+        *count = s->eng->count(s->id);
+        return D4E_OK;
+    });
+}
+
+int d4e_searcher_solutions(d4e_searcher *s, uint64_t max, int32_t single, int8_t *type_grids,
+                           int8_t *step_grids, uint64_t *n) {
+    return guarded([&] {
+        if (!s || !n)
+            return fail(D4E_ERR_INVALID, "null pointer");
+        *n = s->eng->solutions(s->id, max, type_grids, step_grids, single != 0);
+        return D4E_OK;
+    });
+}
+
+int d4e_searcher_level_sizes(const d4e_searcher *s, uint64_t *sizes, uint32_t max, uint32_t *n) {
+    return guarded([&] {
+        if (!s || !n)
+            return fail(D4E_ERR_INVALID, "null pointer");
+        const auto &v = s->eng->level_sizes(s->id);
+        *n = (uint32_t)v.size();
+        for (uint32_t i = 0; sizes && i < max && i < v.size(); i++)
+            sizes[i] = v[i];
+        return D4E_OK;
+    });
+}
+
+static void fill_stats(const d4e::Totals &t, d4e_stats *st) {
+    st->rows = t.steps;
+    st->states_in = t.states_in;
+    st->states_raw = t.states_raw;
+    st->states_out = t.states_out;
+    st->peak_frontier = t.peak_frontier;
+    st->expand_launches = t.expand_launches;
+    st->compact_launches = t.compact_launches;
+    st->retries = t.retries;
+    st->other_launches = t.other_launches;
+    st->h2d_bytes = t.h2d_bytes;
+    st->d2h_bytes = t.d2h_bytes;
+    st->expand_ms = t.expand_ms;
+    st->compact_ms = t.compact_ms;
+    st->run_ms = t.run_ms;
+}
+
+int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st) {
+    return guarded([&] {
+        if (!s || !st)
+            return fail(D4E_ERR_INVALID, "null pointer");
+        fill_stats(s->eng->totals(), st);
+        return D4E_OK;
+    });
+}
+
+int d4e_searcher_set_limit(d4e_searcher *s, uint64_t max_states) {
+    return guarded([&] {
+        if (!s)
+            return fail(D4E_ERR_INVALID, "null searcher");
+        s->eng->set_max_frontier(max_states);
+        return D4E_OK;
+    });
+}
+
+void d4e_searcher_destroy(d4e_searcher *s) { delete s; }
+
+int d4e_batch_count(const d4e_instance *insts, uint32_t n, uint32_t flags, int32_t device,
+                    uint64_t *counts, d4e_stats *st) {
+    return guarded([&] {
+        if ((!insts && n) || (!counts && n))
+            return fail(D4E_ERR_INVALID, "null pointer");
+        d4e::EngineOpts o;
+        o.device = device;
+        d4e::Engine eng(o);
+        auto spec = [&](uint32_t i) {
+            d4e::InstanceSpec sp;
+            sp.width = insts[i].width;
+            sp.height = insts[i].height;
+            sp.rows = insts[i].rows;
+            sp.shapes = insts[i].shapes;
+            sp.counts = insts[i].counts;
+            sp.n_pieces = insts[i].n_pieces;
+            sp.sym = insts[i].sym;
+            return sp;
+        };
+        if (flags & D4E_BATCH_SEQUENTIAL) {
+            for (uint32_t i = 0; i < n; i++) {
+                const uint32_t id = eng.add(spec(i));
+                eng.run();
+                counts[i] = eng.count(id);
+            }
+        } else {
+            std::vector<uint32_t> ids(n);
+            for (uint32_t i = 0; i < n; i++)
+                ids[i] = eng.add(spec(i));
+            eng.run();
+            for (uint32_t i = 0; i < n; i++)
+                counts[i] = eng.count(ids[i]);
+        }
+        if (st)
+            fill_stats(eng.totals(), st);
+        return D4E_OK;
+    });
+}
+
+int d4e_canonical_grid(uint32_t width, uint32_t height, const uint8_t *rows, const int8_t *grid,
+                       int8_t *out) {
+    return guarded([&] {
+        if (!rows || !grid || !out)
+            return fail(D4E_ERR_INVALID, "null pointer");
+        if (width < 1 || width > 8 || height < 1 || height > 64)
+            return fail(D4E_ERR_INVALID, "board size out of range");
+        d4e::canonical_grid(width, height, rows, grid, out);
+        return D4E_OK;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,760 @@
+// engine.cu -- host runtime of the GB300 row-by-row polyomino tiling engine.
+#include "engine.h"
+
+#include <algorithm>
+#include <cstring>
+
+#include "kernels.h"
+
+namespace d4e {
+
+void cuda_check(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        const int code = e == cudaErrorMemoryAllocation ? kErrNoMem : kErrCuda;
+        throw Error(code, std::string(what) + ": " + cudaGetErrorName(e) + ": " +
+                              cudaGetErrorString(e));
+    }
+}
+
+template <class T>
+void DevBuf<T>::reserve(size_t n, cudaStream_t s, size_t keep) {
+    if (n <= cap)
+        return;
+    const size_t nc = std::max(n, cap + cap / 2);
+    T *np = nullptr;
+    cuda_check(cudaMalloc(&np, nc * sizeof(T)), "cudaMalloc");
+    if (p) {
+        if (keep)
+            cuda_check(cudaMemcpyAsync(np, p, keep * sizeof(T), cudaMemcpyDeviceToDevice, s),
+                       "cudaMemcpyAsync");
+        cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        cudaFree(p);
+    }
+    p = np;
+    cap = nc;
+}
+
+template struct DevBuf<Plc>;
+template struct DevBuf<InstDesc>;
+template struct DevBuf<unsigned int>;
+template struct DevBuf<unsigned long long>;
+template struct DevBuf<Seg>;
+template struct DevBuf<ulonglong2>;
+template struct DevBuf<Slot>;
+template struct DevBuf<PathNode>;
+template struct DevBuf<unsigned char>;
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev)
+            cuda_check(cudaSetDevice(dev), "cudaSetDevice");
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev)
+            cudaSetDevice(prev);
+    }
+};
+
+uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
+
+}  // namespace
+
+Engine::Engine(const EngineOpts &opts) : opts_(opts) {
+    int n = 0;
+    cuda_check(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+    if (opts_.device < 0 || opts_.device >= n)
+        throw Error(kErrInvalid, "no such CUDA device");
+    DeviceGuard g(opts_.device);
+    cuda_check(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, opts_.device),
+               "cudaDeviceGetAttribute");
+    cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (auto &e : ev_)
+        cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+    for (auto &e : ev_run_)
+        cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+    misc_.reserve(4, stream_);
+    nraw_.reserve(2, stream_);
+    if (opts_.chunk_states < 32)
+        opts_.chunk_states = 32;
+}
+
+Engine::~Engine() {
+    DeviceGuard g(opts_.device);
+    if (stream_)
+        cudaStreamSynchronize(stream_);
+    for (auto p : lvl_keys_)
+        cudaFree(p);
+    for (auto p : lvl_cnts_)
+        cudaFree(p);
+    for (auto &e : ev_)
+        if (e)
+            cudaEventDestroy(e);
+    for (auto &e : ev_run_)
+        if (e)
+            cudaEventDestroy(e);
+    plc_.release();
+    insts_.release();
+    inst_unique_.release();
+    cursor_.release();
+    results_.release();
+    final_states_.release();
+    misc_.release();
+    nraw_.release();
+    segs_.release();
+    for (int i = 0; i < 2; i++) {
+        keys_[i].release();
+        cnts_[i].release();
+    }
+    table_.release();
+    if (stream_)
+        cudaStreamDestroy(stream_);
+}
+
+void Engine::ensure_inst_capacity(size_t n) {
+    const size_t old = inst_.size();
+    if (n <= insts_.cap)
+        return;
+    insts_.reserve(n, stream_, old);
+    inst_unique_.reserve(n, stream_, 0);
+    cursor_.reserve(n, stream_, 0);
+    results_.reserve(n, stream_, old);
+    final_states_.reserve(n, stream_, old);
+}
+
+uint32_t Engine::add(const InstanceSpec &sp) {
+    DeviceGuard g(opts_.device);
+    if (sp.width < 1 || sp.width > (uint32_t)kMaxWidth)
+        throw Error(kErrInvalid, "board width must be 1..8");
+    if (sp.height < 1 || sp.height > (uint32_t)kMaxHeight)
+        throw Error(kErrInvalid, "board height must be 1..64");
+    if (!sp.rows || (!sp.shapes && sp.n_pieces) || (!sp.counts && sp.n_pieces))
+        throw Error(kErrInvalid, "null pointer in instance");
+    for (uint32_t r = 0; r < sp.height; r++)
+        if (sp.rows[r] >> sp.width)
+            throw Error(kErrInvalid, "board row has cells beyond the width");
+    if (opts_.keep_levels && !inst_.empty())
+        throw Error(kErrState, "an engine keeping levels holds one instance");
+    if (inst_.size() >= kMaxInstances)
+        throw Error(kErrUnsupported, "too many instances");
+
+    Inst in;
+    const std::string err = build_piece_lib(sp.shapes, sp.counts, sp.n_pieces, sp.sym, sp.width,
+                                            in.lib);
+    if (!err.empty())
+        throw Error(err.find("more than") != std::string::npos ? kErrUnsupported : kErrInvalid,
+                    err);
+    const uint32_t id = (uint32_t)inst_.size();
+    in.width = sp.width;
+    in.height = sp.height;
+    InstDesc &d = in.desc;
+    d.width = sp.width;
+    d.height = sp.height;
+    d.win_rows = 64 / sp.width;
+    d.n_plc = (uint32_t)in.lib.plc.size();
+    d.plc_off = (uint32_t)plc_total_;
+    plc_total_ += d.n_plc;
+    for (int c = 0; c < kMaxWidth; c++) {
+        d.col_off[c] = in.lib.col_off[c];
+        d.col_len[c] = in.lib.col_len[c];
+    }
+    std::memset(d.rows, 0, sizeof(d.rows));
+    for (uint32_t r = 0; r < sp.height; r++)
+        d.rows[r] = sp.rows[r];
+    unsigned long long w0 = 0;
+    for (uint32_t r = 0; r < std::min(d.win_rows, sp.height); r++)
+        w0 |= (unsigned long long)sp.rows[r] << (r * sp.width);
+    in.root_k0 = w0;
+    in.root_k1 = kMarker | ((unsigned long long)id << kInstShift);
+
+    ensure_inst_capacity(id + 1);
+    inst_.push_back(std::move(in));
+    pending_.push_back(id);
+    pending_upload_.push_back(id);
+    return id;
+}
+
+void Engine::flush_uploads() {
+    if (pending_upload_.empty())
+        return;
+    // Descriptors and placement tables of newly added instances; ids are
+    // appended in order, so both land in one contiguous range.
+    const uint32_t lo = pending_upload_.front(), hi = pending_upload_.back() + 1;
+    std::vector<InstDesc> descs;
+    descs.reserve(hi - lo);
+    for (uint32_t id = lo; id < hi; id++)
+        descs.push_back(inst_[id].desc);
+    cuda_check(cudaMemcpyAsync(insts_.p + lo, descs.data(), descs.size() * sizeof(InstDesc),
+                               cudaMemcpyHostToDevice, stream_),
+               "upload descriptors");
+    tot_.h2d_bytes += descs.size() * sizeof(InstDesc);
+    // Placement tables are packed back to back in id order.
+    std::vector<Plc> plc;
+    plc.reserve(plc_total_ - plc_uploaded_);
+    for (uint32_t id = lo; id < hi; id++) {
+        const auto &v = inst_[id].lib.plc;
+        plc.insert(plc.end(), v.begin(), v.end());
+    }
+    plc_.reserve(std::max<uint64_t>(plc_total_, 1), stream_, plc_uploaded_);
+    if (!plc.empty())
+        cuda_check(cudaMemcpyAsync(plc_.p + plc_uploaded_, plc.data(), plc.size() * sizeof(Plc),
+                                   cudaMemcpyHostToDevice, stream_),
+                   "upload placements");
+    tot_.h2d_bytes += plc.size() * sizeof(Plc);
+    plc_uploaded_ = plc_total_;
+    cuda_check(cudaMemsetAsync(results_.p + lo, 0, (hi - lo) * sizeof(unsigned long long), stream_),
+               "memset");
+    cuda_check(cudaMemsetAsync(final_states_.p + lo, 0, (hi - lo) * sizeof(unsigned int), stream_),
+               "memset");
+    pending_upload_.clear();
+}
+
+uint64_t Engine::next_size_estimate(uint32_t id) const {
+    const Inst &in = inst_.at(id);
+    if (in.done)
+        return 0;
+    return (uint64_t)((double)std::max<uint64_t>(in.seg_len, 1) * growth_);
+}
+
+StepStats Engine::step() {
+    DeviceGuard g(opts_.device);
+    StepStats st;
+    if (tot_.steps == 0 && !run_started_) {
+        cuda_check(cudaEventRecord(ev_run_[0], stream_), "cudaEventRecord");
+        run_started_ = true;
+    }
+    flush_uploads();
+
+    // Inject root states of newly added instances as new frontier segments.
+    if (!pending_.empty()) {
+        std::vector<ulonglong2> rk;
+        std::vector<unsigned long long> rc;
+        for (uint32_t id : pending_) {
+            Inst &in = inst_[id];
+            in.seg_begin = n_cur_ + rk.size();
+            in.seg_len = 1;
+            in.active = true;
+            n_active_++;
+            active_.push_back(id);
+            rk.push_back(make_ulonglong2(in.root_k0, in.root_k1));
+            rc.push_back(1ull);
+        }
+        keys_[cur_].reserve(n_cur_ + rk.size(), stream_, n_cur_);
+        cnts_[cur_].reserve(n_cur_ + rk.size(), stream_, n_cur_);
+        cuda_check(cudaMemcpyAsync(keys_[cur_].p + n_cur_, rk.data(), rk.size() * sizeof(ulonglong2),
+                                   cudaMemcpyHostToDevice, stream_),
+                   "upload roots");
+        cuda_check(cudaMemcpyAsync(cnts_[cur_].p + n_cur_, rc.data(),
+                                   rc.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                                   stream_),
+                   "upload roots");
+        if (opts_.keep_levels) {
+            ulonglong2 *k = nullptr;
+            unsigned long long *c = nullptr;
+            cuda_check(cudaMalloc(&k, sizeof(ulonglong2)), "cudaMalloc");
+            cuda_check(cudaMalloc(&c, sizeof(unsigned long long)), "cudaMalloc");
+            cuda_check(cudaMemcpyAsync(k, rk.data(), sizeof(ulonglong2), cudaMemcpyHostToDevice,
+                                       stream_),
+                       "upload root");
+            cuda_check(cudaMemcpyAsync(c, rc.data(), sizeof(unsigned long long),
+                                       cudaMemcpyHostToDevice, stream_),
+                       "upload root");
+            lvl_keys_.push_back(k);
+            lvl_cnts_.push_back(c);
+            lvl_n_.push_back(1);
+        }
+        tot_.h2d_bytes += rk.size() * (sizeof(ulonglong2) + sizeof(unsigned long long));
+        n_cur_ += rk.size();
+        pending_.clear();
+    }
+    if (n_active_ == 0)
+        return st;
+
+    // Segments of the active instances, in frontier order.
+    std::sort(active_.begin(), active_.end(),
+              [&](uint32_t a, uint32_t b) { return inst_[a].seg_begin < inst_[b].seg_begin; });
+    std::vector<Seg> segs;
+    segs.reserve(active_.size());
+    uint64_t n_chunks = 0;
+    for (uint32_t id : active_) {
+        const Inst &in = inst_[id];
+        const uint32_t R = in.desc.win_rows, W = in.width;
+        const uint32_t src = in.row + R;
+        const unsigned long long in_row = src < in.height ? in.desc.rows[src] : 0u;
+        Seg s;
+        s.inst = id;
+        s.row = in.row;
+        s.begin = in.seg_begin;
+        s.len = in.seg_len;
+        s.in_shift = in_row << ((R - 1) * W);
+        s.chunk_base = n_chunks;
+        n_chunks += (in.seg_len + opts_.chunk_states - 1) / opts_.chunk_states;
+        segs.push_back(s);
+    }
+    segs_.reserve(segs.size(), stream_);
+    cuda_check(cudaMemcpyAsync(segs_.p, segs.data(), segs.size() * sizeof(Seg),
+                               cudaMemcpyHostToDevice, stream_),
+               "upload segments");
+    tot_.h2d_bytes += segs.size() * sizeof(Seg);
+
+    st.n_in = n_cur_;
+    const uint64_t est = (uint64_t)((double)std::max<uint64_t>(n_cur_, 1) * growth_ /
+                                    opts_.target_load);
+    uint64_t cap = table_capacity(est);
+    const size_t n_inst = inst_.size();
+    h_unique_.assign(n_inst, 0);
+    unsigned int h_status = 0;
+    unsigned long long h_raw = 0;
+    int occ = 0;
+    for (;;) {
+        if (table_.cap < cap) {
+            table_.release();
+            table_clean_ = 0;
+            table_.reserve(cap, stream_);
+        }
+        if (table_clean_ < cap) {
+            cuda_check(cudaMemsetAsync(table_.p + table_clean_, 0,
+                                       (cap - table_clean_) * sizeof(Slot), stream_),
+                       "memset table");
+            table_clean_ = cap;
+        }
+        cuda_check(cudaMemsetAsync(inst_unique_.p, 0, n_inst * sizeof(unsigned int), stream_),
+                   "memset");
+        cuda_check(cudaMemsetAsync(misc_.p, 0, 4 * sizeof(unsigned int), stream_), "memset");
+        cuda_check(cudaMemsetAsync(nraw_.p, 0, 2 * sizeof(unsigned long long), stream_), "memset");
+        ExpandArgs a;
+        a.segs = segs_.p;
+        a.n_segs = (uint32_t)segs.size();
+        a.n_chunks = n_chunks;
+        a.chunk_states = opts_.chunk_states;
+        a.insts = insts_.p;
+        a.plc = plc_.p;
+        a.keys = keys_[cur_].p;
+        a.cnts = cnts_[cur_].p;
+        a.table = table_.p;
+        a.cap = cap;
+        a.inst_unique = inst_unique_.p;
+        a.n_raw = nraw_.p;
+        a.status = misc_.p;
+        a.work = nraw_.p + 1;
+        a.max_probe = opts_.max_probe;
+        if (!occ)
+            occ = expand_occupancy();
+        const int grid = (int)std::min<uint64_t>(n_chunks, (uint64_t)sms_ * (uint64_t)occ);
+        cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
+        launch_expand(a, grid, stream_);
+        cuda_check(cudaGetLastError(), "k_expand launch");
+        cuda_check(cudaEventRecord(ev_[1], stream_), "cudaEventRecord");
+        tot_.expand_launches++;
+        cuda_check(cudaMemcpyAsync(&h_status, misc_.p, sizeof(unsigned int),
+                                   cudaMemcpyDeviceToHost, stream_),
+                   "read status");
+        cuda_check(cudaMemcpyAsync(&h_raw, nraw_.p, sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, stream_),
+                   "read raw");
+        cuda_check(cudaMemcpyAsync(h_unique_.data(), inst_unique_.p, n_inst * sizeof(unsigned int),
+                                   cudaMemcpyDeviceToHost, stream_),
+                   "read unique");
+        cuda_check(cudaStreamSynchronize(stream_), "k_expand");
+        tot_.d2h_bytes += sizeof(unsigned int) + sizeof(unsigned long long) +
+                          n_inst * sizeof(unsigned int);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
+        st.expand_ms += ms;
+        if (!(h_status & kStatusTableOverflow))
+            break;
+        // Table too small for this row: clear it, grow it, redo the row.
+        cuda_check(cudaMemsetAsync(table_.p, 0, cap * sizeof(Slot), stream_), "memset table");
+        uint64_t uniq = 0;
+        for (uint32_t id : active_)
+            uniq += h_unique_[id];
+        const uint64_t want = std::max<uint64_t>(cap * 3, (uint64_t)((double)uniq * 3 / opts_.target_load));
+        const uint64_t grown = table_capacity(want);
+        if (grown <= cap)
+            throw Error(kErrNoMem, "hash table cannot grow: device memory exhausted");
+        cap = grown;
+        st.retries++;
+        tot_.retries++;
+    }
+    st.n_raw = h_raw;
+    st.table_cap = cap;
+    if (opts_.max_frontier) {
+        uint64_t uniq = 0;
+        for (uint32_t id : active_)
+            uniq += h_unique_[id];
+        if (uniq > opts_.max_frontier) {
+            cuda_check(cudaMemsetAsync(table_.p, 0, cap * sizeof(Slot), stream_), "memset table");
+            cuda_check(cudaStreamSynchronize(stream_), "memset table");
+            throw Error(kErrUnsupported, "frontier limit exceeded: " + std::to_string(uniq) +
+                                             " states");
+        }
+    }
+
+    // Next segments: exclusive scan of the per-instance new-key counts.
+    h_cursor_.assign(n_inst, 0ull);
+    uint64_t off = 0;
+    std::vector<std::pair<uint32_t, uint64_t>> nseg;  // (id, begin)
+    std::vector<uint32_t> finishing;
+    for (uint32_t id : active_) {
+        const Inst &in = inst_[id];
+        const uint64_t u = h_unique_[id];
+        st.n_out += u;
+        if (in.row + 1 == in.height && !opts_.keep_levels) {
+            h_cursor_[id] = kCursorFinal;
+            finishing.push_back(id);
+        } else {
+            h_cursor_[id] = off;
+            nseg.push_back({id, off});
+            off += u;
+        }
+    }
+    const int nxt = 1 - cur_;
+    keys_[nxt].reserve(std::max<uint64_t>(off, 1), stream_);
+    cnts_[nxt].reserve(std::max<uint64_t>(off, 1), stream_);
+    cuda_check(cudaMemcpyAsync(cursor_.p, h_cursor_.data(), n_inst * sizeof(unsigned long long),
+                               cudaMemcpyHostToDevice, stream_),
+               "upload cursors");
+    tot_.h2d_bytes += n_inst * sizeof(unsigned long long);
+    CompactArgs c;
+    c.table = table_.p;
+    c.cap = cap;
+    c.cursor = cursor_.p;
+    c.out_keys = keys_[nxt].p;
+    c.out_cnts = cnts_[nxt].p;
+    c.results = results_.p;
+    c.final_states = final_states_.p;
+    const int cgrid = (int)std::min<uint64_t>((cap + 255) / 256, (uint64_t)sms_ * 8);
+    cuda_check(cudaEventRecord(ev_[2], stream_), "cudaEventRecord");
+    launch_compact(c, cgrid, stream_);
+    cuda_check(cudaGetLastError(), "k_compact launch");
+    cuda_check(cudaEventRecord(ev_[3], stream_), "cudaEventRecord");
+    tot_.compact_launches++;
+    if (opts_.keep_levels) {
+        ulonglong2 *k = nullptr;
+        unsigned long long *cn = nullptr;
+        const uint64_t n = std::max<uint64_t>(off, 1);
+        cuda_check(cudaMalloc(&k, n * sizeof(ulonglong2)), "cudaMalloc");
+        cuda_check(cudaMalloc(&cn, n * sizeof(unsigned long long)), "cudaMalloc");
+        if (off) {
+            cuda_check(cudaMemcpyAsync(k, keys_[nxt].p, off * sizeof(ulonglong2),
+                                       cudaMemcpyDeviceToDevice, stream_),
+                       "keep level");
+            cuda_check(cudaMemcpyAsync(cn, cnts_[nxt].p, off * sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToDevice, stream_),
+                       "keep level");
+        }
+        lvl_keys_.push_back(k);
+        lvl_cnts_.push_back(cn);
+        lvl_n_.push_back(off);
+    }
+    cuda_check(cudaEventRecord(ev_run_[1], stream_), "cudaEventRecord");
+    cuda_check(cudaStreamSynchronize(stream_), "k_compact");
+    float cms = 0.f;
+    cudaEventElapsedTime(&cms, ev_[2], ev_[3]);
+    st.compact_ms = cms;
+    float rms = 0.f;
+    cudaEventElapsedTime(&rms, ev_run_[0], ev_run_[1]);
+    tot_.run_ms = rms;
+
+    // Advance the instances.
+    std::vector<uint32_t> still;
+    still.reserve(active_.size());
+    for (const auto &[id, begin] : nseg) {
+        Inst &in = inst_[id];
+        in.seg_begin = begin;
+        in.seg_len = h_unique_[id];
+        in.level_sizes.push_back(in.seg_len);
+        in.row++;
+        if (in.row == in.height || in.seg_len == 0) {
+            in.active = false;
+            in.done = true;
+            n_active_--;
+            if (opts_.keep_levels && in.row == in.height) {
+                std::vector<unsigned long long> cn(in.seg_len);
+                if (in.seg_len)
+                    cuda_check(cudaMemcpy(cn.data(), lvl_cnts_.back(),
+                                          in.seg_len * sizeof(unsigned long long),
+                                          cudaMemcpyDeviceToHost),
+                               "read final level");
+                unsigned long long sum = 0;
+                for (auto v : cn)
+                    sum += v;
+                in.result = sum;
+            } else {
+                in.result = 0;
+            }
+            in.result_ready = true;
+            in.seg_len = 0;
+        } else {
+            still.push_back(id);
+        }
+    }
+    for (uint32_t id : finishing) {
+        Inst &in = inst_[id];
+        in.level_sizes.push_back(h_unique_[id]);
+        in.row++;
+        in.active = false;
+        in.done = true;
+        in.seg_len = 0;
+        n_active_--;
+        unfetched_.push_back(id);
+    }
+    active_.swap(still);
+    n_cur_ = off;
+    cur_ = nxt;
+    if (st.n_in)
+        growth_ = std::clamp((double)st.n_out / (double)st.n_in * 1.25, 1.0, 64.0);
+
+    tot_.steps++;
+    tot_.states_in += st.n_in;
+    tot_.states_raw += st.n_raw;
+    tot_.states_out += st.n_out;
+    tot_.expand_ms += st.expand_ms;
+    tot_.compact_ms += st.compact_ms;
+    tot_.peak_frontier = std::max<uint64_t>(tot_.peak_frontier, st.n_out);
+    return st;
+}
+
+uint64_t Engine::table_capacity(uint64_t want) {
+    // At least 4096 slots, rounded to 1024; never more than the device can
+    // hold next to the frontier buffers (10% of free memory kept back).
+    want = round_up(std::max<uint64_t>(want, 4096), 1024);
+    if (want <= table_.cap)
+        return want;
+    size_t free_b = 0, total_b = 0;
+    cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+    // Room for the next frontier (keys + counts) at the targeted load.
+    const uint64_t next_frontier =
+        (uint64_t)((double)want * opts_.target_load) * (sizeof(ulonglong2) + sizeof(unsigned long long));
+    const uint64_t avail = (uint64_t)table_.cap * sizeof(Slot) + free_b;
+    const uint64_t keep = total_b / 10 + next_frontier;
+    const uint64_t limit = avail > keep ? (avail - keep) / sizeof(Slot) : 0;
+    return std::max<uint64_t>(std::min<uint64_t>(want, limit / 1024 * 1024), 4096);
+}
+
+int Engine::expand_occupancy() {
+    int occ = 0;
+    cuda_check(expand_max_blocks_per_sm(&occ), "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    return std::max(occ, 1);
+}
+
+uint64_t Engine::bucket_count(uint32_t id, uint32_t pattern) {
+    DeviceGuard g(opts_.device);
+    const Inst &in = inst_.at(id);
+    if (!in.active)
+        return 0;
+    const unsigned long long rowmask = (1ull << in.width) - 1ull;
+    cuda_check(cudaMemsetAsync(nraw_.p, 0, sizeof(unsigned long long), stream_), "memset");
+    launch_count_pattern(keys_[cur_].p + in.seg_begin, in.seg_len, rowmask, pattern & rowmask,
+                         nraw_.p, sms_ * 4, stream_);
+    tot_.other_launches++;
+    unsigned long long n = 0;
+    cuda_check(cudaMemcpyAsync(&n, nraw_.p, sizeof(n), cudaMemcpyDeviceToHost, stream_),
+               "read count");
+    cuda_check(cudaStreamSynchronize(stream_), "k_count_pattern");
+    return n;
+}
+
+void Engine::sync_results() {
+    if (unfetched_.empty())
+        return;
+    DeviceGuard g(opts_.device);
+    const uint32_t lo = *std::min_element(unfetched_.begin(), unfetched_.end());
+    const uint32_t hi = *std::max_element(unfetched_.begin(), unfetched_.end()) + 1;
+    std::vector<unsigned long long> r(hi - lo);
+    cuda_check(cudaMemcpyAsync(r.data(), results_.p + lo, r.size() * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, stream_),
+               "read results");
+    tot_.d2h_bytes += r.size() * sizeof(unsigned long long);
+    cuda_check(cudaStreamSynchronize(stream_), "read results");
+    for (uint32_t id : unfetched_) {
+        inst_[id].result = r[id - lo];
+        inst_[id].result_ready = true;
+    }
+    unfetched_.clear();
+}
+
+void Engine::run() {
+    while (has_active())
+        step();
+    sync_results();
+}
+
+uint64_t Engine::count(uint32_t id) {
+    Inst &in = inst_.at(id);
+    if (!in.done)
+        throw Error(kErrState, "instance has not finished");
+    if (!in.result_ready)
+        sync_results();
+    return in.result;
+}
+
+uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t *step_grids,
+                           bool single) {
+    DeviceGuard g(opts_.device);
+    if (!opts_.keep_levels)
+        throw Error(kErrState, "solutions need an engine created with keep_levels");
+    Inst &in = inst_.at(id);
+    if (!in.done)
+        throw Error(kErrState, "instance has not finished");
+    const uint32_t H = in.height;
+    if (in.row < H || count(id) == 0 || max == 0)
+        return 0;
+    if (lvl_n_.size() != (size_t)H + 1)
+        throw Error(kErrState, "level store incomplete");
+
+    // Backward pass: live[r] = states of level r with a child in live[r + 1].
+    std::vector<ulonglong2 *> live(H + 1, nullptr);
+    std::vector<uint64_t> live_n(H + 1, 0);
+    live[H] = lvl_keys_[H];
+    live_n[H] = lvl_n_[H];
+    DevBuf<unsigned char> alive;
+    DevBuf<unsigned long long> nsel;
+    nsel.reserve(1, stream_);
+    std::vector<ulonglong2 *> owned;
+    auto build_set = [&](const ulonglong2 *keys, uint64_t n) -> uint64_t {
+        uint64_t cap = round_up(std::max<uint64_t>(n * 2, 1024), 1024);
+        for (;;) {
+            if (table_.cap < cap) {
+                table_.release();
+                table_.reserve(cap, stream_);
+            }
+            cuda_check(cudaMemsetAsync(table_.p, 0, cap * sizeof(Slot), stream_), "memset");
+            cuda_check(cudaMemsetAsync(misc_.p, 0, sizeof(unsigned int), stream_), "memset");
+            KeySetArgs t{ table_.p, cap, misc_.p, opts_.max_probe };
+            launch_keyset_insert(t, keys, n, sms_ * 4, stream_);
+            unsigned int stt = 0;
+            cuda_check(cudaMemcpyAsync(&stt, misc_.p, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                       stream_),
+                       "read status");
+            cuda_check(cudaStreamSynchronize(stream_), "k_keyset_insert");
+            if (!(stt & kStatusTableOverflow))
+                return cap;
+            cap *= 4;
+        }
+    };
+    auto probe_args = [&](uint32_t r, uint64_t cap) {
+        ProbeArgs p;
+        p.insts = insts_.p;
+        p.plc = plc_.p;
+        p.inst = id;
+        p.row = r;
+        const uint32_t R = in.desc.win_rows, W = in.width, src = r + R;
+        const unsigned long long in_row = src < H ? in.desc.rows[src] : 0u;
+        p.in_shift = in_row << ((R - 1) * W);
+        p.table = table_.p;
+        p.cap = cap;
+        p.max_probe = opts_.max_probe;
+        return p;
+    };
+    for (int r = (int)H - 1; r >= 0; r--) {
+        const uint64_t cap = build_set(live[r + 1], live_n[r + 1]);
+        const uint64_t n = lvl_n_[r];
+        alive.reserve(std::max<uint64_t>(n, 1), stream_);
+        launch_mark_alive(probe_args((uint32_t)r, cap), lvl_keys_[r], n, alive.p, sms_ * 4, stream_);
+        ulonglong2 *out = nullptr;
+        cuda_check(cudaMalloc(&out, std::max<uint64_t>(n, 1) * sizeof(ulonglong2)), "cudaMalloc");
+        owned.push_back(out);
+        cuda_check(cudaMemsetAsync(nsel.p, 0, sizeof(unsigned long long), stream_), "memset");
+        launch_select(lvl_keys_[r], alive.p, n, out, nsel.p, sms_ * 4, stream_);
+        unsigned long long ns = 0;
+        cuda_check(cudaMemcpyAsync(&ns, nsel.p, sizeof(ns), cudaMemcpyDeviceToHost, stream_),
+                   "read select");
+        cuda_check(cudaStreamSynchronize(stream_), "select");
+        live[r] = out;
+        live_n[r] = ns;
+    }
+
+    // Forward pass: extend partial tilings row by row through live states.
+    const uint32_t max_nodes = (uint32_t)std::min<uint64_t>(single ? 1 : max, 1u << 26);
+    std::vector<std::vector<PathNode>> levels(H + 1);
+    PathNode root{};
+    {
+        ulonglong2 rk;
+        cuda_check(cudaMemcpy(&rk, lvl_keys_[0], sizeof(rk), cudaMemcpyDeviceToHost), "read root");
+        root.k0 = rk.x;
+        root.k1 = rk.y;
+        root.parent = ~0u;
+        root.nfill = 0;
+    }
+    levels[0].push_back(root);
+    DevBuf<PathNode> din, dout;
+    DevBuf<unsigned int> dn;
+    dn.reserve(2, stream_);
+    for (uint32_t r = 0; r < H; r++) {
+        const uint64_t cap = build_set(live[r + 1], live_n[r + 1]);
+        const uint32_t n = (uint32_t)levels[r].size();
+        din.reserve(n, stream_);
+        dout.reserve(max_nodes, stream_);
+        cuda_check(cudaMemcpyAsync(din.p, levels[r].data(), n * sizeof(PathNode),
+                                   cudaMemcpyHostToDevice, stream_),
+                   "upload nodes");
+        cuda_check(cudaMemsetAsync(dn.p, 0, 2 * sizeof(unsigned int), stream_), "memset");
+        launch_extend_paths(probe_args(r, cap), din.p, n, dout.p, dn.p, max_nodes, dn.p + 1,
+                            sms_ * 4, stream_);
+        unsigned int hn[2] = {0, 0};
+        cuda_check(cudaMemcpyAsync(hn, dn.p, sizeof(hn), cudaMemcpyDeviceToHost, stream_),
+                   "read nodes");
+        cuda_check(cudaStreamSynchronize(stream_), "extend paths");
+        const uint32_t got = std::min(hn[0], max_nodes);
+        levels[r + 1].resize(got);
+        if (got)
+            cuda_check(cudaMemcpy(levels[r + 1].data(), dout.p, got * sizeof(PathNode),
+                                  cudaMemcpyDeviceToHost),
+                       "read nodes");
+    }
+    for (auto p : owned)
+        cudaFree(p);
+
+    // Leaves -> grids.  Steps are numbered in anchor order (row-major), the
+    // order in which the reference's solver places them.
+    const uint32_t W = in.width, cells = W * H;
+    const auto &lib = in.lib;
+    uint64_t produced = 0;
+    for (const PathNode &leaf : levels[H]) {
+        if (produced >= max)
+            break;
+        std::vector<const PathNode *> chain(H);
+        const PathNode *nd = &leaf;
+        for (int r = (int)H; r >= 1; r--) {
+            chain[r - 1] = nd;
+            nd = r >= 2 ? &levels[r - 1][nd->parent] : nullptr;
+        }
+        int8_t *tg = type_grids ? type_grids + produced * cells : nullptr;
+        int8_t *sg = step_grids ? step_grids + produced * cells : nullptr;
+        for (uint32_t cidx = 0; cidx < cells; cidx++) {
+            if (tg)
+                tg[cidx] = -1;
+            if (sg)
+                sg[cidx] = -1;
+        }
+        int step = 0;
+        for (uint32_t r = 0; r < H; r++) {
+            const PathNode *pn = chain[r];
+            for (uint32_t d = 0; d < pn->nfill; d++, step++) {
+                const uint32_t pi = pn->plc[d];
+                const uint64_t m = lib.plc[pi].mask;
+                for (uint64_t bits = m; bits; bits &= bits - 1) {
+                    const int b = __builtin_ctzll(bits);
+                    const uint32_t cell = r * W + (uint32_t)b;
+                    if (cell < cells) {
+                        if (tg)
+                            tg[cell] = (int8_t)lib.plc_type[pi];
+                        if (sg)
+                            sg[cell] = (int8_t)step;
+                    }
+                }
+            }
+        }
+        produced++;
+    }
+    return produced;
+}
+
+}  // namespace d4e

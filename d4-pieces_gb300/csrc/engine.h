@@ -1,0 +1,199 @@
+// engine.h -- host runtime of the GB300 row-by-row polyomino tiling engine.
+//
+// One Engine drives any number of puzzle instances on one GPU.  Every
+// active instance advances by one board row per step(); the union of their
+// frontiers is expanded by one k_expand launch and compacted by one
+// k_compact launch.  The plain single-puzzle path (CudaSearcher mirror) is an
+// Engine holding one instance; the batched and serving paths add many.
+//
+// Replaces the reference's Device c/m threads, ring buffer and host Sorter
+// (src/device.cu:14-309, src/sorter.cpp:72-214) with device-resident
+// frontier segments and an HBM hash table; no child state crosses PCIe.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "d4e_types.h"
+#include "geometry.h"
+
+namespace d4e {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+enum ErrCode : int {
+    kErrInvalid = -1,
+    kErrCuda = -2,
+    kErrNoMem = -3,
+    kErrUnsupported = -4,
+    kErrState = -5,
+};
+
+void cuda_check(cudaError_t e, const char *what);
+
+// Grow-only device buffer.
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t cap = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    // Ensures capacity >= n elements; keeps the first `keep` elements.
+    void reserve(size_t n, cudaStream_t s, size_t keep = 0);
+};
+
+struct EngineOpts {
+    int device = 0;
+    uint32_t max_probe = 512;
+    bool keep_levels = false;      // retain every level (needed for solutions; one instance)
+    double target_load = 0.5;      // hash table load factor aimed at when sizing
+    uint64_t chunk_states = 1024;  // frontier states per CTA work item
+    uint64_t max_frontier = 0;     // abort when a row yields more states (0 = no limit)
+};
+
+struct InstanceSpec {
+    uint32_t width = 8;
+    uint32_t height = 8;
+    const uint8_t *rows = nullptr;       // height entries, bit c = cell (r, c) to cover
+    const uint64_t *shapes = nullptr;    // Shape<8> layout
+    const uint32_t *counts = nullptr;
+    uint32_t n_pieces = 0;
+    uint32_t sym = 0xFFu;
+};
+
+struct StepStats {
+    uint64_t n_in = 0, n_raw = 0, n_out = 0;
+    float expand_ms = 0.f, compact_ms = 0.f;
+    uint32_t retries = 0;
+    uint64_t table_cap = 0;
+};
+
+struct Totals {
+    uint64_t steps = 0;
+    uint64_t states_in = 0, states_raw = 0, states_out = 0;
+    double expand_ms = 0.0, compact_ms = 0.0;
+    uint64_t expand_launches = 0, compact_launches = 0, other_launches = 0, retries = 0;
+    uint64_t peak_frontier = 0;
+    uint64_t h2d_bytes = 0, d2h_bytes = 0;
+    double run_ms = 0.0;           // CUDA-event time from the first step to the last
+};
+
+class Engine {
+public:
+    explicit Engine(const EngineOpts &opts);
+    ~Engine();
+    Engine(const Engine &) = delete;
+    Engine &operator=(const Engine &) = delete;
+
+    // Adds an instance (validated, tables uploaded); its root state joins the
+    // frontier at the next step().  Returns the instance id.
+    uint32_t add(const InstanceSpec &spec);
+
+    // Advances every active instance by one row.
+    StepStats step();
+    void run();
+    bool has_active() const { return n_active_ > 0 || !pending_.empty(); }
+
+    // Per-instance queries.
+    uint32_t n_instances() const { return (uint32_t)inst_.size(); }
+    bool done(uint32_t id) const { return inst_.at(id).done; }
+    uint32_t row(uint32_t id) const { return inst_.at(id).row; }
+    uint32_t height(uint32_t id) const { return inst_.at(id).height; }
+    uint64_t frontier_size(uint32_t id) const { return inst_.at(id).seg_len; }
+    uint64_t count(uint32_t id);                        // tilings (valid once done)
+    const std::vector<uint64_t> &level_sizes(uint32_t id) const { return inst_.at(id).level_sizes; }
+    uint64_t next_size_estimate(uint32_t id) const;
+    // States of the instance's frontier whose current row equals `pattern`.
+    uint64_t bucket_count(uint32_t id, uint32_t pattern);
+    // Pulls the counts of instances finished since the last call.
+    void sync_results();
+
+    // Solutions of a finished single-instance engine created with
+    // keep_levels.  Writes up to max grids; returns the number of tilings
+    // reconstructed (== the count unless max truncated it).
+    uint64_t solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t *step_grids,
+                       bool single);
+
+    const Totals &totals() const { return tot_; }
+    void set_max_frontier(uint64_t n) { opts_.max_frontier = n; }
+    cudaStream_t stream() const { return stream_; }
+    int sm_count() const { return sms_; }
+
+private:
+    struct Inst {
+        PieceLib lib;
+        InstDesc desc{};
+        uint32_t width = 0, height = 0;
+        uint32_t row = 0;
+        bool active = false, done = false, result_ready = false;
+        uint64_t seg_begin = 0, seg_len = 0;
+        uint64_t result = 0;
+        std::vector<uint64_t> level_sizes;
+        unsigned long long root_k0 = 0, root_k1 = 0;
+    };
+
+    void ensure_inst_capacity(size_t n);
+    void flush_uploads();
+    int expand_occupancy();
+    uint64_t table_capacity(uint64_t want);
+
+    EngineOpts opts_;
+    int sms_ = 0;
+    cudaStream_t stream_ = nullptr;
+    cudaEvent_t ev_[4] = {};
+    cudaEvent_t ev_run_[2] = {};
+
+    std::vector<Inst> inst_;
+    std::vector<uint32_t> pending_;          // roots not yet in the frontier
+    std::vector<uint32_t> pending_upload_;   // descriptors/tables not yet on the device
+    std::vector<uint32_t> active_;           // instances with a frontier segment
+    std::vector<uint32_t> unfetched_;        // finished, result still on the device
+    uint32_t n_active_ = 0;
+
+    DevBuf<Plc> plc_;
+    uint64_t plc_total_ = 0, plc_uploaded_ = 0;
+    DevBuf<InstDesc> insts_;
+    DevBuf<unsigned int> inst_unique_;
+    DevBuf<unsigned long long> cursor_;
+    DevBuf<unsigned long long> results_;
+    DevBuf<unsigned int> final_states_;
+    DevBuf<unsigned int> misc_;   // [0] status, [1] work counter
+    DevBuf<unsigned long long> nraw_;
+    DevBuf<Seg> segs_;
+
+    DevBuf<ulonglong2> keys_[2];
+    DevBuf<unsigned long long> cnts_[2];
+    int cur_ = 0;
+    uint64_t n_cur_ = 0;
+
+    DevBuf<Slot> table_;
+    uint64_t table_clean_ = 0;    // slots [0, table_clean_) are known to be zero
+    double growth_ = 8.0;
+
+    // keep_levels storage: level r = states after completing r rows (r = 0 is the root).
+    std::vector<ulonglong2 *> lvl_keys_;
+    std::vector<unsigned long long *> lvl_cnts_;
+    std::vector<uint64_t> lvl_n_;
+
+    Totals tot_;
+    bool run_started_ = false;
+    std::vector<unsigned int> h_unique_;
+    std::vector<unsigned long long> h_cursor_;
+};
+
+}  // namespace d4e

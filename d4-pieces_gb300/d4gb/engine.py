@@ -1,0 +1,304 @@
+"""ctypes bindings of libd4e.so (include/d4e.h).
+
+Mirrors the reference's host API for the GPU search path:
+``compute_frow_on_cpu`` / ``transfer_frow_to_gpu`` (src/frow.h:10-12) become
+:class:`Frow`, ``CudaSearcher`` (src/searcher_cuda.h:10-38) becomes
+:class:`CudaSearcher`.  Errors raise :class:`D4Error` (the reference throws
+``std::runtime_error``).  There is no CPU fallback: importing this module on a
+machine without the built library raises immediately.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+from typing import Optional, Sequence
+
+import numpy as np
+
+from .build import LIB_PATH
+
+if not LIB_PATH.exists():
+    raise ImportError(f"{LIB_PATH} is missing: build it first (python -c 'import __graft_entry__ as g; g.build()')")
+
+_lib = C.CDLL(str(LIB_PATH))
+
+D4E_OK = 0
+D4E_KEEP_LEVELS = 1
+D4E_BATCH_SEQUENTIAL = 1
+
+_u64p = C.POINTER(C.c_uint64)
+_u32p = C.POINTER(C.c_uint32)
+_u8p = C.POINTER(C.c_uint8)
+_i8p = C.POINTER(C.c_int8)
+
+
+class D4Error(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"d4e error {code}: {msg}")
+        self.code = code
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("rows", C.c_uint64),
+        ("states_in", C.c_uint64),
+        ("states_raw", C.c_uint64),
+        ("states_out", C.c_uint64),
+        ("peak_frontier", C.c_uint64),
+        ("expand_launches", C.c_uint64),
+        ("compact_launches", C.c_uint64),
+        ("retries", C.c_uint64),
+        ("other_launches", C.c_uint64),
+        ("h2d_bytes", C.c_uint64),
+        ("d2h_bytes", C.c_uint64),
+        ("expand_ms", C.c_double),
+        ("compact_ms", C.c_double),
+        ("run_ms", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Instance(C.Structure):
+    _fields_ = [
+        ("width", C.c_uint32),
+        ("height", C.c_uint32),
+        ("rows", _u8p),
+        ("n_pieces", C.c_uint32),
+        ("shapes", _u64p),
+        ("counts", _u32p),
+        ("sym", C.c_uint32),
+    ]
+
+
+def _sig(name, res, *args):
+    f = getattr(_lib, name)
+    f.restype = res
+    f.argtypes = list(args)
+    return f
+
+
+_lib.d4e_last_error.restype = C.c_char_p
+_lib.d4e_version.restype = C.c_char_p
+_sig("d4e_show_gpu_devices", C.c_int)
+_sig("d4e_device_count", C.c_int, C.POINTER(C.c_int32))
+_sig("d4e_catalogue", C.c_int, C.c_uint32, C.c_int32, _u64p, C.c_uint32, _u32p)
+_sig("d4e_frow_create", C.c_int, _u64p, _u32p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32,
+     C.POINTER(C.c_void_p))
+_sig("d4e_frow_transfer", C.c_int, C.c_void_p, C.c_int32)
+_sig("d4e_frow_placements", C.c_int, C.c_void_p, C.c_uint32, _u32p)
+_sig("d4e_frow_destroy", None, C.c_void_p)
+_sig("d4e_searcher_create", C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p))
+_sig("d4e_searcher_create_board", C.c_int, C.c_void_p, C.c_uint32, _u8p, C.c_uint32,
+     C.POINTER(C.c_void_p))
+_sig("d4e_searcher_get_height", C.c_int, C.c_void_p, _u32p)
+_sig("d4e_searcher_size", C.c_int, C.c_void_p, _u64p)
+_sig("d4e_searcher_bucket_size", C.c_int, C.c_void_p, C.c_uint32, _u64p)
+_sig("d4e_searcher_next_size", C.c_int, C.c_void_p, _u64p)
+_sig("d4e_searcher_search_GPU", C.c_int, C.c_void_p)
+_sig("d4e_searcher_run", C.c_int, C.c_void_p)
+_sig("d4e_searcher_count", C.c_int, C.c_void_p, _u64p)
+_sig("d4e_searcher_solutions", C.c_int, C.c_void_p, C.c_uint64, C.c_int32, _i8p, _i8p, _u64p)
+_sig("d4e_searcher_level_sizes", C.c_int, C.c_void_p, _u64p, C.c_uint32, _u32p)
+_sig("d4e_searcher_stats", C.c_int, C.c_void_p, C.POINTER(Stats))
+_sig("d4e_searcher_set_limit", C.c_int, C.c_void_p, C.c_uint64)
+_sig("d4e_searcher_destroy", None, C.c_void_p)
+_sig("d4e_batch_count", C.c_int, C.POINTER(Instance), C.c_uint32, C.c_uint32, C.c_int32, _u64p,
+     C.POINTER(Stats))
+_sig("d4e_canonical_grid", C.c_int, C.c_uint32, C.c_uint32, _u8p, _i8p, _i8p)
+
+
+def lib() -> C.CDLL:
+    return _lib
+
+
+def _check(rc: int) -> None:
+    if rc != D4E_OK:
+        raise D4Error(rc, _lib.d4e_last_error().decode())
+
+
+def _arr(ctype, values):
+    a = (ctype * max(len(values), 1))(*values)
+    return a
+
+
+def version() -> str:
+    return _lib.d4e_version().decode()
+
+
+def device_count() -> int:
+    n = C.c_int32()
+    _check(_lib.d4e_device_count(C.byref(n)))
+    return n.value
+
+
+def show_gpu_devices() -> None:
+    _check(_lib.d4e_show_gpu_devices())
+
+
+def catalogue(m: int, onesided: bool = False) -> list[int]:
+    n = C.c_uint32()
+    _check(_lib.d4e_catalogue(m, int(onesided), None, 0, C.byref(n)))
+    out = (C.c_uint64 * n.value)()
+    _check(_lib.d4e_catalogue(m, int(onesided), out, n.value, C.byref(n)))
+    return list(out)
+
+
+class Frow:
+    """Placement tables of a piece library for boards of one width
+    (compute_frow_on_cpu + transfer_frow_to_gpu)."""
+
+    def __init__(self, shapes: Sequence[int], counts: Sequence[int], sym: int = 0xFF,
+                 width: int = 8, device: Optional[int] = 0, show_report: bool = False):
+        self._h = C.c_void_p()
+        self.shapes = list(shapes)
+        self.counts = list(counts)
+        self.sym = sym
+        self.width = width
+        s = _arr(C.c_uint64, self.shapes)
+        c = _arr(C.c_uint32, self.counts)
+        _check(_lib.d4e_frow_create(s, c, len(self.shapes), sym, width, int(show_report),
+                                    C.byref(self._h)))
+        if device is not None:
+            self.transfer(device)
+
+    def transfer(self, device: int = 0) -> None:
+        _check(_lib.d4e_frow_transfer(self._h, device))
+
+    def placements(self, col: int) -> int:
+        n = C.c_uint32()
+        _check(_lib.d4e_frow_placements(self._h, col, C.byref(n)))
+        return n.value
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.d4e_frow_destroy(self._h)
+            self._h = C.c_void_p()
+
+
+class CudaSearcher:
+    """One puzzle, one board row per :meth:`search_GPU` (src/searcher_cuda.h:10-38)."""
+
+    def __init__(self, frow: Frow, empty_area: Optional[int] = None,
+                 rows: Optional[Sequence[int]] = None, keep_levels: bool = False):
+        self._frow = frow
+        self._h = C.c_void_p()
+        if empty_area is not None:
+            if keep_levels:
+                raise ValueError("keep_levels needs the rows= form")
+            _check(_lib.d4e_searcher_create(frow._h, C.c_uint64(empty_area), C.byref(self._h)))
+            self.width = 8
+            self.rows = [(empty_area >> (8 * r)) & 0xFF for r in range(8)]
+            while self.rows and self.rows[-1] == 0:
+                self.rows.pop()
+        else:
+            self.rows = list(rows)
+            self.width = frow.width
+            r = _arr(C.c_uint8, self.rows)
+            _check(_lib.d4e_searcher_create_board(frow._h, len(self.rows), r,
+                                                  D4E_KEEP_LEVELS if keep_levels else 0,
+                                                  C.byref(self._h)))
+        self.height = len(self.rows)
+
+    def get_height(self) -> int:
+        v = C.c_uint32()
+        _check(_lib.d4e_searcher_get_height(self._h, C.byref(v)))
+        return v.value
+
+    def size(self, bucket: Optional[int] = None) -> int:
+        v = C.c_uint64()
+        if bucket is None:
+            _check(_lib.d4e_searcher_size(self._h, C.byref(v)))
+        else:
+            _check(_lib.d4e_searcher_bucket_size(self._h, bucket, C.byref(v)))
+        return v.value
+
+    def next_size(self) -> int:
+        v = C.c_uint64()
+        _check(_lib.d4e_searcher_next_size(self._h, C.byref(v)))
+        return v.value
+
+    def search_GPU(self) -> None:
+        _check(_lib.d4e_searcher_search_GPU(self._h))
+
+    def run(self) -> None:
+        _check(_lib.d4e_searcher_run(self._h))
+
+    def count(self) -> int:
+        v = C.c_uint64()
+        _check(_lib.d4e_searcher_count(self._h, C.byref(v)))
+        return v.value
+
+    def level_sizes(self) -> list[int]:
+        n = C.c_uint32()
+        _check(_lib.d4e_searcher_level_sizes(self._h, None, 0, C.byref(n)))
+        buf = (C.c_uint64 * max(n.value, 1))()
+        _check(_lib.d4e_searcher_level_sizes(self._h, buf, n.value, C.byref(n)))
+        return list(buf)[: n.value]
+
+    def solutions(self, max_solutions: int, single: bool = False):
+        """(type_grids, step_grids) as int8 arrays of shape (n, height, width)."""
+        cells = self.width * self.height
+        tg = np.full((max(max_solutions, 1), cells), -1, dtype=np.int8)
+        sg = np.full((max(max_solutions, 1), cells), -1, dtype=np.int8)
+        n = C.c_uint64()
+        _check(_lib.d4e_searcher_solutions(self._h, max_solutions, int(single),
+                                           tg.ctypes.data_as(_i8p), sg.ctypes.data_as(_i8p),
+                                           C.byref(n)))
+        k = n.value
+        return (tg[:k].reshape(k, self.height, self.width),
+                sg[:k].reshape(k, self.height, self.width))
+
+    def set_limit(self, max_states: int) -> None:
+        _check(_lib.d4e_searcher_set_limit(self._h, max_states))
+
+    def stats(self) -> dict:
+        st = Stats()
+        _check(_lib.d4e_searcher_stats(self._h, C.byref(st)))
+        return st.as_dict()
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.d4e_searcher_destroy(self._h)
+            self._h = C.c_void_p()
+
+
+def _instances(problems) -> tuple:
+    arr = (Instance * max(len(problems), 1))()
+    keep = []
+    for i, p in enumerate(problems):
+        rows = _arr(C.c_uint8, p.rows)
+        shapes = _arr(C.c_uint64, p.shapes)
+        counts = _arr(C.c_uint32, p.counts)
+        keep += [rows, shapes, counts]
+        arr[i] = Instance(p.width, p.height, C.cast(rows, _u8p), len(p.shapes),
+                          C.cast(shapes, _u64p), C.cast(counts, _u32p), p.sym)
+    return arr, keep
+
+
+def batch_count(problems, sequential: bool = False, device: int = 0):
+    """Counts for a list of problems; returns (counts, stats dict)."""
+    arr, keep = _instances(problems)
+    out = (C.c_uint64 * max(len(problems), 1))()
+    st = Stats()
+    _check(_lib.d4e_batch_count(arr, len(problems), D4E_BATCH_SEQUENTIAL if sequential else 0,
+                                device, out, C.byref(st)))
+    return list(out)[: len(problems)], st.as_dict()
+
+
+def count(problem, device: int = 0) -> int:
+    """Tilings of one problem through the plain searcher path."""
+    f = Frow(problem.shapes, problem.counts, problem.sym, problem.width, device)
+    s = CudaSearcher(f, rows=problem.rows)
+    s.run()
+    return s.count()
+
+
+def canonical_grid(problem, grid) -> np.ndarray:
+    g = np.ascontiguousarray(np.asarray(grid, dtype=np.int8).reshape(-1))
+    out = np.empty_like(g)
+    rows = _arr(C.c_uint8, problem.rows)
+    _check(_lib.d4e_canonical_grid(problem.width, problem.height, rows,
+                                   g.ctypes.data_as(_i8p), out.ctypes.data_as(_i8p)))
+    return out.reshape(problem.height, problem.width)

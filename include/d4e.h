@@ -1,0 +1,212 @@
+/*
+ * d4e.h -- C ABI of the GB300 (sm_103a) row-by-row polyomino tiling engine.
+ *
+ * Drop-in boundary for the reference's GPU search path (b1f6c1c4/d4-pieces,
+ * src/searcher_cuda.h, src/frow.h).  Plain pointers and sizes only; every
+ * entry point returns D4E_OK (0) or a negative error code, with the message
+ * available from d4e_last_error() (the reference throws std::runtime_error
+ * from THROW / C(), src/util.hpp:73-74, src/util.cuh:23-40; the C++ facade in
+ * d4-pieces_gb300/host/searcher_cuda.h turns the codes back into exceptions).
+ *
+ * Board layout: rows of up to 8 cells; bit c of row r set = cell (r, c) must
+ * be covered.  The reference's `uint64_t empty_area` is the same layout for
+ * an 8-wide board of up to 8 rows (bit 8*r + c, src/searcher_cuda.h:11).
+ * Piece shapes use the reference's Shape<8> layout (bit 8*r + c,
+ * src/Shape.hpp:20-24); `sym` selects transforms in Shape::transforms()
+ * order (0xFF = all eight D4 transforms, 0x69 = rotations only).
+ *
+ * Results are exact: the number of tilings of the board by a sub-multiset of
+ * the pieces (copies of one piece type are indistinguishable), as the
+ * reference's CPU solver solve_count (src/Piece.cpp:104-139) counts them.
+ *
+ * Threading: one thread at a time per handle; distinct handles may be used
+ * concurrently.  The library owns all device memory it allocates; callers
+ * own their host buffers.
+ */
+#ifndef D4E_H
+#define D4E_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define D4E_OK 0
+#define D4E_ERR_INVALID (-1)     /* bad argument */
+#define D4E_ERR_CUDA (-2)        /* CUDA runtime error (no device, launch failure, ...) */
+#define D4E_ERR_NOMEM (-3)       /* device memory exhausted */
+#define D4E_ERR_UNSUPPORTED (-4) /* outside the engine's limits (see below) */
+#define D4E_ERR_STATE (-5)       /* call not valid in the handle's current state */
+
+/* Limits: board width 1..8, height 1..64, <= 40 piece copies per puzzle,
+ * <= 255 placements anchored at one column, pieces no taller than 64/width
+ * rows. */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *d4e_last_error(void);
+
+/* Library version string. */
+const char *d4e_version(void);
+
+/* Number of visible CUDA devices (0 when there is no driver or device); the
+ * reference's transfer_frow_to_gpu counts them with cudaGetDeviceCount
+ * (src/frow.cu:8-12). */
+int d4e_device_count(int32_t *n);
+
+/* Prints the CUDA devices (reference: show_gpu_devices, src/frow.cu:37-90). */
+int d4e_show_gpu_devices(void);
+
+/* ------------------------------------------------------------------------
+ * Piece catalogue (reference: known_shapes / known_C_shapes, src/known.hpp:9-19,
+ * src/known1.cpp, src/known2.cpp).  Canonical polyominoes of m cells
+ * (m = 1..8) sorted by value; onesided != 0 selects the one-sided set.
+ * Writes up to max values; *n receives the catalogue size.
+ * ---------------------------------------------------------------------- */
+int d4e_catalogue(uint32_t m, int32_t onesided, uint64_t *out, uint32_t max, uint32_t *n);
+
+/* ------------------------------------------------------------------------
+ * Placement ("frow") tables.
+ * ---------------------------------------------------------------------- */
+typedef struct d4e_frow d4e_frow;
+
+/* Builds the placement tables of a piece library for boards of the given
+ * width: every allowed orientation of every piece anchored at every column.
+ * Replaces compute_frow_on_cpu(bool show_report) (src/frow.h:10,
+ * src/frow.cpp:39-166), which reads the piece set from the globals g_nme /
+ * g_sym; here the pieces are explicit.  show_report != 0 prints the
+ * per-column placement counts like the reference's report. */
+int d4e_frow_create(const uint64_t *shapes, const uint32_t *counts, uint32_t n_pieces,
+                    uint32_t sym, uint32_t width, int32_t show_report, d4e_frow **out);
+
+/* Binds the tables to a CUDA device (they are uploaded into each searcher's
+ * device table slot when the searcher is created).  Replaces
+ * transfer_frow_to_gpu() (src/frow.h:11, src/frow.cu:7-35); fails with
+ * D4E_ERR_CUDA "no CUDA device" like the reference. */
+int d4e_frow_transfer(d4e_frow *f, int32_t device);
+
+/* Number of placements anchored at column col (the reference reports
+ * h_frowInfoL/R[..].sz, src/frow.h:41-48). */
+int d4e_frow_placements(const d4e_frow *f, uint32_t col, uint32_t *n);
+
+void d4e_frow_destroy(d4e_frow *f);
+
+/* ------------------------------------------------------------------------
+ * Searcher: one puzzle, one board row per search_GPU() call.
+ * Reference: struct CudaSearcher (src/searcher_cuda.h:10-38,
+ * src/searcher_cuda.cu:12-90).
+ * ---------------------------------------------------------------------- */
+typedef struct d4e_searcher d4e_searcher;
+
+#define D4E_KEEP_LEVELS 1u   /* retain every row's frontier: enables d4e_searcher_solutions */
+
+/* CudaSearcher(uint64_t empty_area): 8-wide board, height = number of rows up
+ * to the last cell to cover (src/searcher_cuda.cu:12-21).  The frow tables
+ * must have width 8 and have been transferred. */
+int d4e_searcher_create(const d4e_frow *f, uint64_t empty_area, d4e_searcher **out);
+
+/* Board of any height 1..64 with the frow tables' width; flags = 0 or
+ * D4E_KEEP_LEVELS. */
+int d4e_searcher_create_board(const d4e_frow *f, uint32_t height, const uint8_t *rows,
+                              uint32_t flags, d4e_searcher **out);
+
+/* Rows still to be completed (CudaSearcher::get_height). */
+int d4e_searcher_get_height(const d4e_searcher *s, uint32_t *height);
+
+/* Current frontier size in states (CudaSearcher::size()). */
+int d4e_searcher_size(const d4e_searcher *s, uint64_t *n);
+
+/* States of the current frontier whose current row equals the 8-bit pattern
+ * `bucket` (CudaSearcher::size(unsigned i), the reference's 256 row-byte
+ * buckets). */
+int d4e_searcher_bucket_size(d4e_searcher *s, uint32_t bucket, uint64_t *n);
+
+/* Estimated size of the next frontier (CudaSearcher::next_size()). */
+int d4e_searcher_next_size(const d4e_searcher *s, uint64_t *n);
+
+/* Completes one board row: expands every state by every whole-row fill and
+ * de-duplicates the children on the device (CudaSearcher::search_GPU). */
+int d4e_searcher_search_GPU(d4e_searcher *s);
+
+/* Runs search_GPU until the height reaches 0. */
+int d4e_searcher_run(d4e_searcher *s);
+
+/* Number of tilings; valid once the height is 0. */
+int d4e_searcher_count(d4e_searcher *s, uint64_t *count);
+
+/* Tilings of a finished searcher created with D4E_KEEP_LEVELS, reconstructed
+ * on the device from the per-row frontiers.  Each solution is a W*H grid of
+ * piece type ids (type_grids) and of step indices in placement order
+ * (step_grids), -1 outside the board, like the reference's
+ * Solution::map + Step::piece_id (src/Piece.hpp:31-48).  single != 0 returns
+ * one tiling (reference solve(..., single = true)).  Either grid pointer may
+ * be NULL.  *n receives the number written (<= max). */
+int d4e_searcher_solutions(d4e_searcher *s, uint64_t max, int32_t single, int8_t *type_grids,
+                           int8_t *step_grids, uint64_t *n);
+
+/* Per-row frontier sizes (states after each completed row); writes up to max
+ * entries, *n receives the number of completed rows. */
+int d4e_searcher_level_sizes(const d4e_searcher *s, uint64_t *sizes, uint32_t max, uint32_t *n);
+
+typedef struct d4e_stats {
+    uint64_t rows;              /* search_GPU steps run */
+    uint64_t states_in;         /* frontier states expanded (sum over rows) */
+    uint64_t states_raw;        /* children produced before de-duplication */
+    uint64_t states_out;        /* distinct children (sum over rows) */
+    uint64_t peak_frontier;     /* largest frontier */
+    uint64_t expand_launches;   /* k_expand launches (including table-growth retries) */
+    uint64_t compact_launches;  /* k_compact launches */
+    uint64_t retries;           /* rows redone after a table overflow */
+    uint64_t other_launches;    /* other kernels (bucket counts, ...) */
+    uint64_t h2d_bytes;         /* host-to-device bytes copied by the engine */
+    uint64_t d2h_bytes;         /* device-to-host bytes copied by the engine */
+    double expand_ms;           /* device time of k_expand (CUDA events) */
+    double compact_ms;          /* device time of k_compact (CUDA events) */
+    double run_ms;              /* CUDA-event time from the first row's start to the last row's end */
+} d4e_stats;
+
+int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st);
+
+/* Makes search_GPU fail with D4E_ERR_UNSUPPORTED once a row would produce
+ * more than max_states distinct states (0 = no limit), a guard for
+ * exploratory runs; the reference sizes its ring buffer from free memory
+ * instead (src/device.cu:30-32). */
+int d4e_searcher_set_limit(d4e_searcher *s, uint64_t max_states);
+
+void d4e_searcher_destroy(d4e_searcher *s);
+
+/* ------------------------------------------------------------------------
+ * Batches: many independent puzzles.  The reference runs one CudaSearcher per
+ * board configuration from a thread pool (SearcherFactory::run,
+ * src/searcher.cpp:86-107).
+ * ---------------------------------------------------------------------- */
+typedef struct d4e_instance {
+    uint32_t width;             /* 1..8 */
+    uint32_t height;            /* 1..64 */
+    const uint8_t *rows;        /* height row masks */
+    uint32_t n_pieces;
+    const uint64_t *shapes;     /* Shape<8> layout */
+    const uint32_t *counts;     /* copies per piece type */
+    uint32_t sym;               /* allowed transforms */
+} d4e_instance;
+
+#define D4E_BATCH_SEQUENTIAL 1u /* one puzzle at a time, one launch sequence per puzzle */
+
+/* Counts the tilings of every instance.  Default: all instances advance
+ * together, one k_expand + one k_compact launch per board row for the whole
+ * batch.  With D4E_BATCH_SEQUENTIAL each instance runs alone (the plain
+ * per-puzzle path).  counts[i] receives instance i's count.  st may be NULL. */
+int d4e_batch_count(const d4e_instance *insts, uint32_t n, uint32_t flags, int32_t device,
+                    uint64_t *counts, d4e_stats *st);
+
+/* Canonical D4 form of a solution type grid over the board's own symmetry
+ * (lexicographic minimum over the transforms mapping the board onto
+ * itself). */
+int d4e_canonical_grid(uint32_t width, uint32_t height, const uint8_t *rows, const int8_t *grid,
+                       int8_t *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* D4E_H */

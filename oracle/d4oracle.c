@@ -1,0 +1,689 @@
+/*
+ * d4oracle.c -- CPU oracle (TEST INFRASTRUCTURE ONLY; see d4oracle.h).
+ *
+ * Restates, in plain C, the reference's CPU backtracking solver and its
+ * row-by-row level search.  Each function cites the reference file:line it
+ * follows.  The product library never links or calls this file.
+ */
+#include "d4oracle.h"
+
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+typedef unsigned __int128 u128;
+
+#define OR_MAX_TYPES 128
+#define OR_MAX_COPIES 64
+
+/* ------------------------------------------------------------------------
+ * Shape<8> geometry on a uint64 (bit 8*r + c), reference src/Shape.hpp:182-191
+ * (normalize) and src/Shape.cpp:6-40 (transform / transforms order).
+ * ---------------------------------------------------------------------- */
+static uint64_t s8_normalize(uint64_t v)
+{
+    if (!v)
+        return 0;
+    while (!(v & 0xFFull))
+        v >>= 8;
+    while (!(v & 0x0101010101010101ull))
+        v >>= 1;
+    return v;
+}
+
+/* Transform index t follows Shape::transforms(): bit0 = FlipX, bit1 = FlipY,
+ * bit2 = Swap; out(r,c) = in(ir,ic) (src/Shape.cpp:12-21), then normalize. */
+static uint64_t s8_transform(uint64_t v, int t)
+{
+    int sw = (t >> 2) & 1, fx = t & 1, fy = (t >> 1) & 1;
+    uint64_t out = 0;
+    for (int r = 0; r < 8; r++)
+        for (int c = 0; c < 8; c++) {
+            int ir = sw ? c : r, ic = sw ? r : c;
+            if (fx)
+                ic = 7 - ic;
+            if (fy)
+                ir = 7 - ir;
+            if ((v >> (ir * 8 + ic)) & 1u)
+                out |= 1ull << (r * 8 + c);
+        }
+    return s8_normalize(out);
+}
+
+static int popc128(u128 v)
+{
+    return __builtin_popcountll((uint64_t)v) + __builtin_popcountll((uint64_t)(v >> 64));
+}
+
+static int ctz128(u128 v)
+{
+    uint64_t lo = (uint64_t)v;
+    return lo ? __builtin_ctzll(lo) : 64 + __builtin_ctzll((uint64_t)(v >> 64));
+}
+
+/* ------------------------------------------------------------------------
+ * Piece library, reference src/Piece.cpp:12-22 (Piece::Piece): one entry per
+ * transform allowed by `sym`, in transforms() order; a transform equal to an
+ * earlier one is kept but disabled.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+    uint64_t normal;   /* normalized Shape<8> value */
+    int h, w;          /* bounding box */
+    int enabled;
+    int ncells;
+    int cr[64], cc[64]; /* cells in increasing bit order (Shape iteration) */
+} or_plc;
+
+typedef struct {
+    uint32_t count;
+    int size;
+    int nplc;
+    or_plc plc[8];
+} or_piece;
+
+typedef struct {
+    int W, H;
+    u128 board;
+    int n;
+    or_piece *lib;
+} or_ctx;
+
+static int build_ctx(const or_problem *p, or_ctx *c)
+{
+    if (!p || p->width < 1 || p->width > 11 || p->height < 1 ||
+        p->width * p->height > 128 || p->n_pieces < 0 || p->n_pieces > OR_MAX_TYPES)
+        return -1;
+    c->W = p->width;
+    c->H = p->height;
+    c->n = p->n_pieces;
+    c->board = 0;
+    for (int r = 0; r < c->H; r++)
+        for (int x = 0; x < c->W; x++)
+            if ((p->rows[r] >> x) & 1u)
+                c->board |= (u128)1 << (r * c->W + x);
+    c->lib = (or_piece *)calloc(c->n ? c->n : 1, sizeof(or_piece));
+    for (int i = 0; i < c->n; i++) {
+        or_piece *pc = &c->lib[i];
+        uint64_t s = p->shapes[i];
+        if (!s) {
+            free(c->lib);
+            return -1;
+        }
+        pc->count = p->counts[i];
+        pc->size = __builtin_popcountll(s);
+        pc->nplc = 0;
+        unsigned sym = p->sym;
+        for (int t = 0; t < 8; t++, sym >>= 1) {
+            if (!(sym & 1u))
+                continue;
+            uint64_t sh = s8_transform(s, t);
+            or_plc *pl = &pc->plc[pc->nplc++];
+            pl->normal = sh;
+            pl->enabled = 1;
+            for (int k = 0; k < pc->nplc - 1; k++)
+                if (pc->plc[k].normal == sh)
+                    pl->enabled = 0;
+            pl->h = pl->w = 0;
+            pl->ncells = 0;
+            for (int b = 0; b < 64; b++)
+                if ((sh >> b) & 1u) {
+                    int r = b / 8, x = b % 8;
+                    pl->cr[pl->ncells] = r;
+                    pl->cc[pl->ncells] = x;
+                    pl->ncells++;
+                    if (r + 1 > pl->h)
+                        pl->h = r + 1;
+                    if (x + 1 > pl->w)
+                        pl->w = x + 1;
+                }
+        }
+    }
+    return 0;
+}
+
+/* Placement cell mask with its top-left corner at (y, x) of the W-stride board. */
+static u128 plc_mask(const or_ctx *c, const or_plc *pl, int y, int x)
+{
+    u128 m = 0;
+    for (int k = 0; k < pl->ncells; k++)
+        m |= (u128)1 << ((pl->cr[k] + y) * c->W + pl->cc[k] + x);
+    return m;
+}
+
+/* ------------------------------------------------------------------------
+ * Backtracking solver, reference src/Piece.cpp:57-139 and src/Piece.inl:5-24.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+    or_ctx *c;
+    uint32_t used[OR_MAX_TYPES];
+    int max_tiles;
+    uint64_t count;
+    /* solve() */
+    int single;
+    int64_t nsol, maxsol;
+    int nstep;
+    int step_type[128];
+    u128 step_mask[128];
+    int8_t *type_grids, *step_grids;
+} or_search;
+
+/* min_tiles, src/Piece.cpp:57-63 */
+static int min_tiles(const or_search *s)
+{
+    int m = 1 << 30;
+    for (int i = 0; i < s->c->n; i++)
+        if (s->used[i] < s->c->lib[i].count && s->c->lib[i].size < m)
+            m = s->c->lib[i].size;
+    return m;
+}
+
+static void record_solution(or_search *s)
+{
+    if (s->nsol < s->maxsol) {
+        int cells = s->c->W * s->c->H;
+        int8_t *tg = s->type_grids ? s->type_grids + s->nsol * cells : NULL;
+        int8_t *sg = s->step_grids ? s->step_grids + s->nsol * cells : NULL;
+        for (int cell = 0; cell < cells; cell++) {
+            int id = -1;
+            for (int k = 0; k < s->nstep; k++)
+                if ((s->step_mask[k] >> cell) & 1u) {
+                    id = k;
+                    break;
+                }
+            if (tg)
+                tg[cell] = (int8_t)(id < 0 ? -1 : s->step_type[id]);
+            if (sg)
+                sg[cell] = (int8_t)id;
+        }
+    }
+    s->nsol++;
+}
+
+/* The recursive lambda `f` of solve / solve_count.  Returns 1 to stop
+ * (solve with single == true found a solution). */
+static int search_rec(or_search *s, u128 open, int want_solutions)
+{
+    const or_ctx *c = s->c;
+    int sz = popc128(open);
+    if (sz > s->max_tiles)
+        return 0;
+    if (!open) {
+        if (want_solutions) {
+            record_solution(s);
+            return s->single;
+        }
+        s->count++;
+        return 0;
+    }
+    if (sz < min_tiles(s))
+        return 0;
+    int pos = ctz128(open);
+    int ty = pos / c->W, tx = pos % c->W;
+    for (int id = 0; id < c->n; id++) {
+        const or_piece *pc = &c->lib[id];
+        if (s->used[id] == pc->count)
+            continue;
+        s->used[id]++;
+        s->max_tiles -= pc->size;
+        /* Piece::cover(pos, func), src/Piece.inl:5-24: every enabled
+         * placement, every cell of it as the one landing on pos. */
+        for (int t = 0; t < pc->nplc; t++) {
+            const or_plc *pl = &pc->plc[t];
+            if (!pl->enabled)
+                continue;
+            for (int k = 0; k < pl->ncells; k++) {
+                int x = tx - pl->cc[k], y = ty - pl->cr[k];
+                if (x < 0 || y < 0 || x + pl->w > c->W || y + pl->h > c->H)
+                    continue;
+                u128 placed = plc_mask(c, pl, y, x);
+                if (placed & ~open)
+                    continue;
+                if (want_solutions) {
+                    s->step_type[s->nstep] = id;
+                    s->step_mask[s->nstep] = placed;
+                    s->nstep++;
+                }
+                int stop = search_rec(s, open & ~placed, want_solutions);
+                if (want_solutions)
+                    s->nstep--;
+                if (stop)
+                    return 1;
+            }
+        }
+        s->max_tiles += pc->size;
+        s->used[id]--;
+    }
+    return 0;
+}
+
+static void init_search(or_search *s, or_ctx *c)
+{
+    memset(s, 0, sizeof(*s));
+    s->c = c;
+    for (int i = 0; i < c->n; i++)
+        s->max_tiles += c->lib[i].size * (int)c->lib[i].count;
+}
+
+int64_t or_solve_count(const or_problem *p)
+{
+    or_ctx c;
+    if (build_ctx(p, &c))
+        return -1;
+    or_search *s = (or_search *)malloc(sizeof(or_search));
+    init_search(s, &c);
+    search_rec(s, c.board, 0);
+    int64_t r = (int64_t)s->count;
+    free(s);
+    free(c.lib);
+    return r;
+}
+
+int64_t or_solve(const or_problem *p, int32_t single, int64_t max_solutions,
+                 int8_t *type_grids, int8_t *step_grids)
+{
+    or_ctx c;
+    if (build_ctx(p, &c))
+        return -1;
+    or_search *s = (or_search *)malloc(sizeof(or_search));
+    init_search(s, &c);
+    s->single = single ? 1 : 0;
+    s->maxsol = max_solutions;
+    s->type_grids = type_grids;
+    s->step_grids = step_grids;
+    search_rec(s, c.board, 1);
+    int64_t r = s->nsol;
+    free(s);
+    free(c.lib);
+    return r;
+}
+
+/* ------------------------------------------------------------------------
+ * Canonical D4 form of a solution grid.  The reference has no solution
+ * canonicalisation; this applies Shape::transform's cell mapping
+ * (src/Shape.cpp:12-21) to the W x H grid and keeps the transforms that map
+ * the board onto itself.
+ * ---------------------------------------------------------------------- */
+void or_canonical_grid(const or_problem *p, const int8_t *grid, int8_t *out)
+{
+    int W = p->width, H = p->height, cells = W * H;
+    int8_t tmp[128];
+    int have = 0;
+    for (int t = 0; t < 8; t++) {
+        int sw = (t >> 2) & 1, fx = t & 1, fy = (t >> 1) & 1;
+        if (sw && W != H)
+            continue;
+        int ok = 1;
+        for (int r = 0; r < H && ok; r++)
+            for (int x = 0; x < W; x++) {
+                int ir = sw ? x : r, ic = sw ? r : x;
+                if (fx)
+                    ic = W - 1 - ic;
+                if (fy)
+                    ir = H - 1 - ir;
+                int a = (p->rows[r] >> x) & 1u, b = (p->rows[ir] >> ic) & 1u;
+                if (a != b) {
+                    ok = 0;
+                    break;
+                }
+                tmp[r * W + x] = grid[ir * W + ic];
+            }
+        if (!ok)
+            continue;
+        /* lexicographic over signed cell values */
+        int less = !have;
+        for (int i = 0; have && i < cells; i++)
+            if (tmp[i] != out[i]) {
+                less = tmp[i] < out[i];
+                break;
+            }
+        if (less)
+            memcpy(out, tmp, (size_t)cells);
+        have = 1;
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Exact row-by-row frontier DP (restating the level structure of
+ * src/searcher_cuda.cu:32-82 and the per-record expansion of
+ * src/kernel.cuh:12-49 with whole-row fills).
+ * State = (open cells of the whole board, used-copy mask).  Copies of a type
+ * occupy a contiguous bit range and are taken lowest-free-first, so the mask
+ * encodes the per-type used counts.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+    u128 open;
+    uint64_t used;
+    uint64_t cnt;
+} dp_state;
+
+typedef struct {
+    dp_state *v;
+    size_t n, cap;
+} dp_vec;
+
+static void vec_push(dp_vec *a, const dp_state *s)
+{
+    if (a->n == a->cap) {
+        a->cap = a->cap ? a->cap * 2 : 1024;
+        a->v = (dp_state *)realloc(a->v, a->cap * sizeof(dp_state));
+    }
+    a->v[a->n++] = *s;
+}
+
+typedef struct {
+    uint64_t rel;   /* placement mask relative to its row, anchored at column col */
+    uint64_t rel_hi;
+    uint64_t tmask; /* copy bits of its piece type */
+    int h;          /* rows spanned */
+} dp_plc;
+
+typedef struct {
+    int W, H, T;
+    u128 board;
+    int nplc[11];
+    dp_plc *plc[11];
+} dp_tab;
+
+static uint64_t mix64(uint64_t x)
+{
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdull;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ull;
+    x ^= x >> 33;
+    return x;
+}
+
+static uint64_t dp_hash(const dp_state *s)
+{
+    return mix64((uint64_t)s->open ^ mix64((uint64_t)(s->open >> 64) ^ mix64(s->used)));
+}
+
+typedef struct {
+    const dp_tab *tab;
+    int row;
+    dp_vec *shards; /* T shard buffers for this worker */
+    int T;
+    uint64_t cnt;
+} dp_expand_ctx;
+
+static void dp_fill(dp_expand_ctx *e, u128 open, uint64_t used)
+{
+    const dp_tab *t = e->tab;
+    int W = t->W;
+    u128 rowm = (((u128)1 << W) - 1) << (e->row * W);
+    if (!(open & rowm)) {
+        dp_state s = { open, used, e->cnt };
+        vec_push(&e->shards[dp_hash(&s) % (uint64_t)e->T], &s);
+        return;
+    }
+    int pos = ctz128(open);
+    int col = pos % W;
+    for (int i = 0; i < t->nplc[col]; i++) {
+        const dp_plc *pl = &t->plc[col][i];
+        if (e->row + pl->h > t->H)
+            continue;
+        u128 m = (((u128)pl->rel_hi << 64) | pl->rel) << (e->row * W);
+        if (m & ~open)
+            continue;
+        uint64_t tm = pl->tmask;
+        uint64_t nb = ((used & tm) + (tm & (~tm + 1))) & tm;
+        if (!nb)
+            continue;
+        dp_fill(e, open & ~m, used | nb);
+    }
+}
+
+typedef struct {
+    const dp_tab *tab;
+    int row, T, id;
+    const dp_state *in;
+    size_t lo, hi;
+    dp_vec **shards; /* [worker][shard] */
+    dp_vec *out;     /* per shard output */
+} dp_job;
+
+static void *dp_expand_worker(void *arg)
+{
+    dp_job *j = (dp_job *)arg;
+    dp_expand_ctx e;
+    e.tab = j->tab;
+    e.row = j->row;
+    e.T = j->T;
+    e.shards = j->shards[j->id];
+    for (size_t i = j->lo; i < j->hi; i++) {
+        e.cnt = j->in[i].cnt;
+        dp_fill(&e, j->in[i].open, j->in[i].used);
+    }
+    return NULL;
+}
+
+static void *dp_merge_worker(void *arg)
+{
+    dp_job *j = (dp_job *)arg;
+    size_t total = 0;
+    for (int w = 0; w < j->T; w++)
+        total += j->shards[w][j->id].n;
+    size_t cap = 16;
+    while (cap < total * 2)
+        cap *= 2;
+    dp_state *tab = (dp_state *)calloc(cap, sizeof(dp_state));
+    unsigned char *occ = (unsigned char *)calloc(cap, 1);
+    dp_vec *out = &j->out[j->id];
+    out->n = 0;
+    for (int w = 0; w < j->T; w++) {
+        dp_vec *v = &j->shards[w][j->id];
+        for (size_t i = 0; i < v->n; i++) {
+            const dp_state *s = &v->v[i];
+            size_t h = (size_t)(mix64(dp_hash(s)) & (cap - 1));
+            for (;;) {
+                if (!occ[h]) {
+                    occ[h] = 1;
+                    tab[h] = *s;
+                    break;
+                }
+                if (tab[h].open == s->open && tab[h].used == s->used) {
+                    tab[h].cnt += s->cnt;
+                    break;
+                }
+                h = (h + 1) & (cap - 1);
+            }
+        }
+        v->n = 0;
+    }
+    for (size_t h = 0; h < cap; h++)
+        if (occ[h])
+            vec_push(out, &tab[h]);
+    free(tab);
+    free(occ);
+    return NULL;
+}
+
+static double now_s(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+int32_t or_rowdp(const or_problem *p, int32_t threads, double max_seconds,
+                 uint64_t *level_sizes, uint64_t *count,
+                 int32_t *levels_done, uint64_t *states_total)
+{
+    or_ctx c;
+    if (build_ctx(p, &c))
+        return -1;
+    if (threads < 1)
+        threads = 1;
+    int copies = 0;
+    for (int i = 0; i < c.n; i++)
+        copies += (int)c.lib[i].count;
+    if (copies > OR_MAX_COPIES) {
+        free(c.lib);
+        return -1;
+    }
+    dp_tab tab;
+    memset(&tab, 0, sizeof(tab));
+    tab.W = c.W;
+    tab.H = c.H;
+    tab.board = c.board;
+    /* Placements anchored at (row 0, col): anchor = lowest cell. */
+    int base = 0;
+    for (int i = 0; i < c.n; i++) {
+        const or_piece *pc = &c.lib[i];
+        uint64_t tm = pc->count ? (((pc->count >= 64) ? ~0ull : ((1ull << pc->count) - 1)) << base) : 0;
+        base += (int)pc->count;
+        for (int t = 0; t < pc->nplc; t++) {
+            const or_plc *pl = &pc->plc[t];
+            if (!pl->enabled || !tm)
+                continue;
+            for (int col = 0; col < c.W; col++) {
+                int x = col - pl->cc[0];
+                if (x < 0 || x + pl->w > c.W || pl->h > c.H)
+                    continue;
+                u128 m = plc_mask(&c, pl, 0, x);
+                tab.plc[col] = (dp_plc *)realloc(tab.plc[col], (size_t)(tab.nplc[col] + 1) * sizeof(dp_plc));
+                dp_plc *d = &tab.plc[col][tab.nplc[col]++];
+                d->rel = (uint64_t)m;
+                d->rel_hi = (uint64_t)(m >> 64);
+                d->tmask = tm;
+                d->h = pl->h;
+            }
+        }
+    }
+    int T = threads;
+    dp_vec cur = { 0, 0, 0 };
+    dp_state root = { c.board, 0, 1 };
+    vec_push(&cur, &root);
+    dp_vec **shards = (dp_vec **)calloc((size_t)T, sizeof(dp_vec *));
+    for (int w = 0; w < T; w++)
+        shards[w] = (dp_vec *)calloc((size_t)T, sizeof(dp_vec));
+    dp_vec *outs = (dp_vec *)calloc((size_t)T, sizeof(dp_vec));
+    dp_job *jobs = (dp_job *)calloc((size_t)T, sizeof(dp_job));
+    pthread_t *th = (pthread_t *)calloc((size_t)T, sizeof(pthread_t));
+    double t0 = now_s();
+    uint64_t tot = 0;
+    int done = 0;
+    for (int r = 0; r < c.H; r++) {
+        for (int w = 0; w < T; w++) {
+            jobs[w].tab = &tab;
+            jobs[w].row = r;
+            jobs[w].T = T;
+            jobs[w].id = w;
+            jobs[w].in = cur.v;
+            jobs[w].lo = cur.n * (size_t)w / (size_t)T;
+            jobs[w].hi = cur.n * (size_t)(w + 1) / (size_t)T;
+            jobs[w].shards = shards;
+            jobs[w].out = outs;
+        }
+        if (T == 1)
+            dp_expand_worker(&jobs[0]);
+        else {
+            for (int w = 0; w < T; w++)
+                pthread_create(&th[w], NULL, dp_expand_worker, &jobs[w]);
+            for (int w = 0; w < T; w++)
+                pthread_join(th[w], NULL);
+        }
+        if (T == 1)
+            dp_merge_worker(&jobs[0]);
+        else {
+            for (int w = 0; w < T; w++)
+                pthread_create(&th[w], NULL, dp_merge_worker, &jobs[w]);
+            for (int w = 0; w < T; w++)
+                pthread_join(th[w], NULL);
+        }
+        cur.n = 0;
+        for (int w = 0; w < T; w++)
+            for (size_t i = 0; i < outs[w].n; i++)
+                vec_push(&cur, &outs[w].v[i]);
+        if (level_sizes)
+            level_sizes[r] = cur.n;
+        tot += cur.n;
+        done = r + 1;
+        if (max_seconds > 0 && now_s() - t0 > max_seconds)
+            break;
+    }
+    uint64_t cnt = 0;
+    if (done == c.H)
+        for (size_t i = 0; i < cur.n; i++)
+            cnt += cur.v[i].cnt;
+    if (count)
+        *count = cnt;
+    if (levels_done)
+        *levels_done = done;
+    if (states_total)
+        *states_total = tot;
+    for (int w = 0; w < T; w++) {
+        for (int s = 0; s < T; s++)
+            free(shards[w][s].v);
+        free(shards[w]);
+        free(outs[w].v);
+    }
+    free(shards);
+    free(outs);
+    free(jobs);
+    free(th);
+    free(cur.v);
+    for (int col = 0; col < 11; col++)
+        free(tab.plc[col]);
+    free(c.lib);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------
+ * Independent cover check (used for solve-one answers).
+ * ---------------------------------------------------------------------- */
+int32_t or_check_tiling(const or_problem *p, int32_t n, const int32_t *types,
+                        const uint64_t *mask_lo, const uint64_t *mask_hi)
+{
+    or_ctx c;
+    if (build_ctx(p, &c))
+        return 0;
+    uint32_t used[OR_MAX_TYPES];
+    memset(used, 0, sizeof(used));
+    u128 acc = 0;
+    int ok = 1;
+    for (int i = 0; i < n && ok; i++) {
+        int t = types[i];
+        u128 m = ((u128)mask_hi[i] << 64) | mask_lo[i];
+        if (t < 0 || t >= c.n || !m || (m & acc)) {
+            ok = 0;
+            break;
+        }
+        acc |= m;
+        if (++used[t] > c.lib[t].count) {
+            ok = 0;
+            break;
+        }
+        int minr = 1 << 30, minc = 1 << 30;
+        for (int b = 0; b < c.W * c.H; b++)
+            if ((m >> b) & 1u) {
+                if (b / c.W < minr)
+                    minr = b / c.W;
+                if (b % c.W < minc)
+                    minc = b % c.W;
+            }
+        uint64_t v = 0;
+        for (int b = 0; b < c.W * c.H && ok; b++)
+            if ((m >> b) & 1u) {
+                int r = b / c.W - minr, x = b % c.W - minc;
+                if (r >= 8 || x >= 8)
+                    ok = 0;
+                else
+                    v |= 1ull << (r * 8 + x);
+            }
+        if (!ok)
+            break;
+        int match = 0;
+        for (int k = 0; k < c.lib[t].nplc; k++)
+            if (c.lib[t].plc[k].normal == v)
+                match = 1;
+        if (!match)
+            ok = 0;
+    }
+    if (ok && acc != c.board)
+        ok = 0;
+    free(c.lib);
+    return ok;
+}
