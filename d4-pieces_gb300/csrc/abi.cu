@@ -306,7 +306,8 @@ int d4e_searcher_level_sizes(const d4e_searcher *s, uint64_t *sizes, uint32_t ma
     });
 }
 
-static void fill_stats(const d4e::Totals &t, d4e_stats *st) {
+static void fill_stats(const d4e::Engine &e, d4e_stats *st) {
+    const d4e::Totals &t = e.totals();
     st->rows = t.steps;
     st->states_in = t.states_in;
     st->states_raw = t.states_raw;
@@ -321,13 +322,15 @@ static void fill_stats(const d4e::Totals &t, d4e_stats *st) {
     st->expand_ms = t.expand_ms;
     st->compact_ms = t.compact_ms;
     st->run_ms = t.run_ms;
+    st->record_bytes = e.packed_keys() ? 16 : 24;
+    st->slot_bytes = e.packed_keys() ? 16 : 32;
 }
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st) {
     return guarded([&] {
         if (!s || !st)
             return fail(D4E_ERR_INVALID, "null pointer");
-        fill_stats(s->eng->totals(), st);
+        fill_stats(*s->eng, st);
         return D4E_OK;
     });
 }
@@ -377,7 +380,7 @@ int d4e_batch_count(const d4e_instance *insts, uint32_t n, uint32_t flags, int32
                 counts[i] = eng.count(ids[i]);
         }
         if (st)
-            fill_stats(eng.totals(), st);
+            fill_stats(eng, st);
         return D4E_OK;
     });
 }

@@ -1,18 +1,22 @@
 // d4e_types.h -- data layouts shared by the host runtime and the sm_103a kernels.
 //
-// Frontier state (one per distinct partial tiling class at a row boundary):
-//   key.x = window : 64-bit row-aligned occupancy window.  Bit (i*W + c) set
-//                    means cell (row+i, c) still has to be covered, for the
-//                    R = 64 / W board rows starting at the current row.
-//   key.y = tag    : bits 0..39   used piece copies (copies of one type take a
-//                                 contiguous bit range and are used
-//                                 lowest-free-first, so the mask is the
-//                                 per-type used-count vector),
-//                    bits 40..62  instance id,
-//                    bit  63      marker (a valid key is never all-zero).
-//   count          : number of partial tilings reaching this state (u64).
-// Keys and counts are stored structure-of-arrays: keys as 16-byte
-// ulonglong2 (128-bit coalesced loads/stores), counts as u64.
+// A frontier state is (row window, used piece copies) plus the number of
+// partial tilings reaching it.
+//   window : bit i*W + c set = cell (row+i, c) still has to be covered, for
+//            the R = 64 / W board rows starting at the current row.
+//   used   : per piece type a binary counter of copies placed, in a bit
+//            field of bit_length(count) bits (fields packed from bit 0;
+//            <= 40 bits in all).
+// Two encodings of the key, chosen per engine:
+//   K64  (packed, used whenever it fits): key = the window's first
+//        W*(max piece rows - 1) bits (the only rows earlier placements can
+//        reach; deeper rows are the board's) | used << those bits |
+//        instance id << inst_off | marker bit 63.  Record = {key, count},
+//        16 bytes; table slot 16 bytes; 64-bit CAS.
+//   K128 (general): key.x = full 64-bit window, key.y = used (bits 0..39) |
+//        instance id (bits 40..62) | marker (bit 63).  Record = 16-byte key +
+//        8-byte count; table slot 32 bytes; 128-bit CAS.
+// The marker bit makes every valid key non-zero, so a zeroed table is empty.
 //
 // This replaces the reference's 20/24-byte R/RX records (src/record.h:5-32),
 // whose packing of <= 16 used piece names and an 8-row window is exact only
@@ -25,19 +29,29 @@ namespace d4e {
 
 constexpr int kMaxWidth = 8;          // 8-wide boards, as the reference's frow tables
 constexpr int kMaxHeight = 64;        // rows per board
-constexpr int kMaxCopies = 40;        // piece copies per instance (bits 0..39 of the tag)
-constexpr int kInstShift = 40;        // instance id position in the tag
+constexpr int kMaxUsedBits = 40;      // bits of all per-type copy counters together
+constexpr int kMaxTypes = kMaxUsedBits;
+constexpr int kInstShift128 = 40;     // instance id position in a K128 key's second word
 constexpr uint32_t kMaxInstances = 1u << 23;
 constexpr int kMaxPlcPerCol = 255;    // placements anchored at one column (8-bit DFS stack)
 constexpr int kMaxPlc = kMaxWidth * kMaxPlcPerCol;
 constexpr uint64_t kMarker = 1ull << 63;
-constexpr uint64_t kUsedMask = (1ull << kInstShift) - 1;
+constexpr uint64_t kUsedMask128 = (1ull << kInstShift128) - 1;
 
-// One placement anchored at a column of the current row: `mask` holds its
-// cells in window coordinates (bit i*W + c), `tm` the copy bits of its type.
+// One placement anchored at a column of the current row: its cells in window
+// coordinates (bit i*W + c) and its piece type.
 struct Plc {
     uint64_t mask;
-    uint64_t tm;
+    uint32_t type;
+    uint32_t pad;
+};
+
+// Copy counter of one piece type: field mask and capacity (count << offset),
+// both in `used` coordinates.  A copy is available when (used & fm) < cap;
+// taking it adds the field's lowest bit.
+struct TypeField {
+    uint64_t fm;
+    uint64_t cap;
 };
 
 // Per-instance constants, resident in device memory.
@@ -47,9 +61,12 @@ struct InstDesc {
     uint32_t win_rows;    // R = 64 / width
     uint32_t n_plc;
     uint32_t plc_off;     // first placement in the global placement array
-    uint32_t pad0;
+    uint32_t n_types;
+    uint32_t dyn_bits;    // width * (max piece rows - 1): window bits a K64 key keeps
+    uint32_t used_bits;
     uint16_t col_off[kMaxWidth];   // placements anchored at column c: [col_off, col_off + col_len)
     uint16_t col_len[kMaxWidth];
+    TypeField types[kMaxTypes];
     uint8_t rows[kMaxHeight];      // board rows, bit c = cell to cover
 };
 
@@ -57,20 +74,25 @@ struct InstDesc {
 // of `chunk_states` states; chunk_base is the global index of its first chunk.
 struct Seg {
     uint32_t inst;
-    uint32_t row;         // row being completed
+    uint32_t row;                 // row being completed
     uint64_t begin;
     uint64_t len;
-    uint64_t in_shift;    // board row (row + R) placed in window row R-1 after the shift
     uint64_t chunk_base;
+    unsigned long long in_shift;  // K128: board row (row + R) entering window row R-1
+    unsigned long long hi_board;  // K64: board rows [row + dyn_rows, row + R) in window coordinates
+    unsigned long long tag;       // instance id bits | marker, in the mode's key coordinates
 };
 
-// Open-addressing hash table slot (32 bytes = one DRAM sector).  An all-zero
-// key is empty; valid keys always carry the marker bit.
-struct alignas(32) Slot {
+// Hash table slots.  A zero key is empty.
+struct alignas(32) Slot32 {
     unsigned long long k0;
     unsigned long long k1;
     unsigned long long cnt;
     unsigned long long pad;
+};
+struct alignas(16) Slot16 {
+    unsigned long long key;
+    unsigned long long cnt;
 };
 
 // Device status word bits.
@@ -85,8 +107,8 @@ constexpr unsigned long long kCursorFinal = ~0ull;
 
 // Solution path node (one completed row of one partial tiling).
 struct PathNode {
-    unsigned long long k0, k1;   // state after the row
-    uint32_t parent;             // node index in the previous row's list (~0u at row 0)
+    unsigned long long k0, k1;   // state after the row (K64: k1 = 0)
+    uint32_t parent;             // node index in the previous row's list
     uint32_t nfill;              // placements used to complete the row
     uint16_t plc[kMaxWidth];     // placement index (instance-relative) per fill step
 };

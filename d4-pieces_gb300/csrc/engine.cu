@@ -41,7 +41,6 @@ template struct DevBuf<unsigned int>;
 template struct DevBuf<unsigned long long>;
 template struct DevBuf<Seg>;
 template struct DevBuf<ulonglong2>;
-template struct DevBuf<Slot>;
 template struct DevBuf<PathNode>;
 template struct DevBuf<unsigned char>;
 
@@ -63,6 +62,15 @@ struct DeviceGuard {
 };
 
 uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
+
+uint32_t bit_length(uint64_t v) {
+    uint32_t b = 0;
+    while (v) {
+        b++;
+        v >>= 1;
+    }
+    return b;
+}
 
 }  // namespace
 
@@ -92,7 +100,8 @@ Engine::~Engine() {
     for (auto p : lvl_keys_)
         cudaFree(p);
     for (auto p : lvl_cnts_)
-        cudaFree(p);
+        if (p)
+            cudaFree(p);
     for (auto &e : ev_)
         if (e)
             cudaEventDestroy(e);
@@ -151,6 +160,9 @@ uint32_t Engine::add(const InstanceSpec &sp) {
         throw Error(err.find("more than") != std::string::npos ? kErrUnsupported : kErrInvalid,
                     err);
     const uint32_t id = (uint32_t)inst_.size();
+    if (mode_fixed_ && k64_ && n_active_ > 0 &&
+        (in.lib.dyn_bits + in.lib.used_bits > inst_off_ || id > inst_mask_))
+        throw Error(kErrUnsupported, "instance does not fit the engine's packed key layout");
     in.width = sp.width;
     in.height = sp.height;
     InstDesc &d = in.desc;
@@ -159,25 +171,50 @@ uint32_t Engine::add(const InstanceSpec &sp) {
     d.win_rows = 64 / sp.width;
     d.n_plc = (uint32_t)in.lib.plc.size();
     d.plc_off = (uint32_t)plc_total_;
+    d.n_types = (uint32_t)in.lib.fields.size();
+    d.dyn_bits = in.lib.dyn_bits;
+    d.used_bits = in.lib.used_bits;
     plc_total_ += d.n_plc;
     for (int c = 0; c < kMaxWidth; c++) {
         d.col_off[c] = in.lib.col_off[c];
         d.col_len[c] = in.lib.col_len[c];
     }
+    for (uint32_t t = 0; t < d.n_types; t++)
+        d.types[t] = in.lib.fields[t];
     std::memset(d.rows, 0, sizeof(d.rows));
     for (uint32_t r = 0; r < sp.height; r++)
         d.rows[r] = sp.rows[r];
     unsigned long long w0 = 0;
     for (uint32_t r = 0; r < std::min(d.win_rows, sp.height); r++)
         w0 |= (unsigned long long)sp.rows[r] << (r * sp.width);
-    in.root_k0 = w0;
-    in.root_k1 = kMarker | ((unsigned long long)id << kInstShift);
+    in.root_window = w0;
 
     ensure_inst_capacity(id + 1);
     inst_.push_back(std::move(in));
     pending_.push_back(id);
     pending_upload_.push_back(id);
     return id;
+}
+
+void Engine::fix_key_mode() {
+    // The encoding is chosen while no state is resident (first step, or any
+    // step after every instance has finished), from the instances waiting to
+    // start; later additions must fit it (checked in add()).
+    if (mode_fixed_ && (n_active_ > 0 || pending_.empty()))
+        return;
+    uint32_t need = 0, max_id = 0;
+    for (uint32_t id : pending_) {
+        need = std::max(need, inst_[id].lib.dyn_bits + inst_[id].lib.used_bits);
+        max_id = std::max(max_id, id);
+    }
+    const uint32_t ibits = bit_length(max_id);
+    const bool fits = need + ibits <= 63;
+    if (opts_.key_mode == KeyMode::K64 && !fits)
+        throw Error(kErrUnsupported, "packed 64-bit keys do not fit these instances");
+    k64_ = opts_.key_mode == KeyMode::K64 || (opts_.key_mode == KeyMode::Auto && fits);
+    inst_off_ = need;
+    inst_mask_ = ibits ? ((1ull << ibits) - 1ull) : 0ull;
+    mode_fixed_ = true;
 }
 
 void Engine::flush_uploads() {
@@ -212,6 +249,8 @@ void Engine::flush_uploads() {
                "memset");
     cuda_check(cudaMemsetAsync(final_states_.p + lo, 0, (hi - lo) * sizeof(unsigned int), stream_),
                "memset");
+    // The host staging vectors die here: make sure the copies have read them.
+    cuda_check(cudaStreamSynchronize(stream_), "upload tables");
     pending_upload_.clear();
 }
 
@@ -222,9 +261,72 @@ uint64_t Engine::next_size_estimate(uint32_t id) const {
     return (uint64_t)((double)std::max<uint64_t>(in.seg_len, 1) * growth_);
 }
 
+// Per-row constants of one instance's segment, in the engine's key encoding.
+Seg Engine::seg_for(uint32_t id, uint32_t row) const {
+    const Inst &in = inst_[id];
+    const uint32_t R = in.desc.win_rows, W = in.width;
+    Seg s{};
+    s.inst = id;
+    s.row = row;
+    const uint32_t src = row + R;
+    const unsigned long long in_row = src < in.height ? in.desc.rows[src] : 0u;
+    s.in_shift = in_row << ((R - 1) * W);
+    const uint32_t dyn_rows = W ? in.lib.dyn_bits / W : 0;
+    unsigned long long hi = 0;
+    for (uint32_t i = dyn_rows; i < R; i++) {
+        const uint32_t r = row + i;
+        if (r < in.height)
+            hi |= (unsigned long long)in.desc.rows[r] << (i * W);
+    }
+    s.hi_board = hi;
+    s.tag = k64_ ? (kMarker | ((unsigned long long)id << inst_off_))
+                 : (kMarker | ((unsigned long long)id << kInstShift128));
+    return s;
+}
+
+ulonglong2 Engine::root_record(uint32_t id) const {
+    const Inst &in = inst_[id];
+    if (k64_) {
+        const unsigned long long dynmask = (1ull << in.lib.dyn_bits) - 1ull;
+        return make_ulonglong2((in.root_window & dynmask) | kMarker |
+                                   ((unsigned long long)id << inst_off_),
+                               1ull);
+    }
+    return make_ulonglong2(in.root_window, kMarker | ((unsigned long long)id << kInstShift128));
+}
+
+uint64_t Engine::table_capacity(uint64_t want) {
+    // At least 1M slots (16-32 MB: cheap to clear, avoids regrowing on small
+    // rows), rounded to 1024; never more than the device can hold next to
+    // the next frontier (10% of the device kept back).
+    want = round_up(std::max<uint64_t>(want, 1ull << 20), 1024);
+    const uint64_t slot_bytes = slot_units() * sizeof(ulonglong2);
+    if (want * slot_units() <= table_.cap)
+        return want;
+    size_t free_b = 0, total_b = 0;
+    cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+    const uint64_t rec_bytes = k64_ ? 16 : 24;
+    const uint64_t next_frontier = (uint64_t)((double)want * opts_.target_load) * rec_bytes;
+    const uint64_t avail = (uint64_t)table_.cap * sizeof(ulonglong2) + free_b;
+    const uint64_t keep = total_b / 10 + next_frontier;
+    const uint64_t limit = avail > keep ? (avail - keep) / slot_bytes : 0;
+    return std::max<uint64_t>(std::min<uint64_t>(want, limit / 1024 * 1024), 1ull << 20);
+}
+
+int Engine::expand_occupancy() {
+    int &occ = k64_ ? occ64_ : occ128_;
+    if (!occ) {
+        cuda_check(expand_max_blocks_per_sm(k64_, &occ),
+                   "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        occ = std::max(occ, 1);
+    }
+    return occ;
+}
+
 StepStats Engine::step() {
     DeviceGuard g(opts_.device);
     StepStats st;
+    fix_key_mode();
     if (tot_.steps == 0 && !run_started_) {
         cuda_check(cudaEventRecord(ev_run_[0], stream_), "cudaEventRecord");
         run_started_ = true;
@@ -242,34 +344,41 @@ StepStats Engine::step() {
             in.active = true;
             n_active_++;
             active_.push_back(id);
-            rk.push_back(make_ulonglong2(in.root_k0, in.root_k1));
+            rk.push_back(root_record(id));
             rc.push_back(1ull);
         }
         keys_[cur_].reserve(n_cur_ + rk.size(), stream_, n_cur_);
-        cnts_[cur_].reserve(n_cur_ + rk.size(), stream_, n_cur_);
         cuda_check(cudaMemcpyAsync(keys_[cur_].p + n_cur_, rk.data(), rk.size() * sizeof(ulonglong2),
                                    cudaMemcpyHostToDevice, stream_),
                    "upload roots");
-        cuda_check(cudaMemcpyAsync(cnts_[cur_].p + n_cur_, rc.data(),
-                                   rc.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
-                                   stream_),
-                   "upload roots");
+        tot_.h2d_bytes += rk.size() * sizeof(ulonglong2);
+        if (!k64_) {
+            cnts_[cur_].reserve(n_cur_ + rk.size(), stream_, n_cur_);
+            cuda_check(cudaMemcpyAsync(cnts_[cur_].p + n_cur_, rc.data(),
+                                       rc.size() * sizeof(unsigned long long),
+                                       cudaMemcpyHostToDevice, stream_),
+                       "upload roots");
+            tot_.h2d_bytes += rc.size() * sizeof(unsigned long long);
+        }
         if (opts_.keep_levels) {
             ulonglong2 *k = nullptr;
             unsigned long long *c = nullptr;
             cuda_check(cudaMalloc(&k, sizeof(ulonglong2)), "cudaMalloc");
-            cuda_check(cudaMalloc(&c, sizeof(unsigned long long)), "cudaMalloc");
             cuda_check(cudaMemcpyAsync(k, rk.data(), sizeof(ulonglong2), cudaMemcpyHostToDevice,
                                        stream_),
                        "upload root");
-            cuda_check(cudaMemcpyAsync(c, rc.data(), sizeof(unsigned long long),
-                                       cudaMemcpyHostToDevice, stream_),
-                       "upload root");
+            if (!k64_) {
+                cuda_check(cudaMalloc(&c, sizeof(unsigned long long)), "cudaMalloc");
+                cuda_check(cudaMemcpyAsync(c, rc.data(), sizeof(unsigned long long),
+                                           cudaMemcpyHostToDevice, stream_),
+                           "upload root");
+            }
             lvl_keys_.push_back(k);
             lvl_cnts_.push_back(c);
             lvl_n_.push_back(1);
         }
-        tot_.h2d_bytes += rk.size() * (sizeof(ulonglong2) + sizeof(unsigned long long));
+        // rk / rc are pageable: wait until the copies have read them.
+        cuda_check(cudaStreamSynchronize(stream_), "upload roots");
         n_cur_ += rk.size();
         pending_.clear();
     }
@@ -279,22 +388,33 @@ StepStats Engine::step() {
     // Segments of the active instances, in frontier order.
     std::sort(active_.begin(), active_.end(),
               [&](uint32_t a, uint32_t b) { return inst_[a].seg_begin < inst_[b].seg_begin; });
+    // Small frontiers (fewer states than a quarter of the resident lanes) are
+    // split: each state's walk is cut by its first placement into `fan` work
+    // items, so a handful of states still spreads over the whole GPU.
+    int occ = expand_occupancy();
+    const uint64_t slots = (uint64_t)sms_ * (uint64_t)occ;
+    uint32_t fan = 0;
+    if (n_cur_ * 4 < slots * 256) {
+        for (uint32_t id : active_)
+            for (int c = 0; c < kMaxWidth; c++)
+                fan = std::max<uint32_t>(fan, inst_[id].desc.col_len[c]);
+        fan = std::max<uint32_t>(fan, 1);
+    }
+    const uint64_t items = n_cur_ * (fan ? fan : 1);
+    // Chunk size: about four chunks per resident CTA, within [64, chunk_states].
+    uint64_t chunk = (items + 4 * slots - 1) / (4 * slots);
+    chunk = std::min<uint64_t>(std::max<uint64_t>(round_up(chunk, 64), 64), opts_.chunk_states);
     std::vector<Seg> segs;
     segs.reserve(active_.size());
     uint64_t n_chunks = 0;
+    const uint64_t per = fan ? fan : 1;
     for (uint32_t id : active_) {
         const Inst &in = inst_[id];
-        const uint32_t R = in.desc.win_rows, W = in.width;
-        const uint32_t src = in.row + R;
-        const unsigned long long in_row = src < in.height ? in.desc.rows[src] : 0u;
-        Seg s;
-        s.inst = id;
-        s.row = in.row;
-        s.begin = in.seg_begin;
-        s.len = in.seg_len;
-        s.in_shift = in_row << ((R - 1) * W);
+        Seg s = seg_for(id, in.row);
+        s.begin = in.seg_begin * per;
+        s.len = in.seg_len * per;
         s.chunk_base = n_chunks;
-        n_chunks += (in.seg_len + opts_.chunk_states - 1) / opts_.chunk_states;
+        n_chunks += (s.len + chunk - 1) / chunk;
         segs.push_back(s);
     }
     segs_.reserve(segs.size(), stream_);
@@ -311,18 +431,18 @@ StepStats Engine::step() {
     h_unique_.assign(n_inst, 0);
     unsigned int h_status = 0;
     unsigned long long h_raw = 0;
-    int occ = 0;
     for (;;) {
-        if (table_.cap < cap) {
+        const uint64_t units = cap * slot_units();
+        if (table_.cap < units) {
             table_.release();
             table_clean_ = 0;
-            table_.reserve(cap, stream_);
+            table_.reserve(units, stream_);
         }
-        if (table_clean_ < cap) {
+        if (table_clean_ < units) {
             cuda_check(cudaMemsetAsync(table_.p + table_clean_, 0,
-                                       (cap - table_clean_) * sizeof(Slot), stream_),
+                                       (units - table_clean_) * sizeof(ulonglong2), stream_),
                        "memset table");
-            table_clean_ = cap;
+            table_clean_ = units;
         }
         cuda_check(cudaMemsetAsync(inst_unique_.p, 0, n_inst * sizeof(unsigned int), stream_),
                    "memset");
@@ -332,10 +452,11 @@ StepStats Engine::step() {
         a.segs = segs_.p;
         a.n_segs = (uint32_t)segs.size();
         a.n_chunks = n_chunks;
-        a.chunk_states = opts_.chunk_states;
+        a.chunk_states = chunk;
+        a.fan = fan;
         a.insts = insts_.p;
         a.plc = plc_.p;
-        a.keys = keys_[cur_].p;
+        a.recs = keys_[cur_].p;
         a.cnts = cnts_[cur_].p;
         a.table = table_.p;
         a.cap = cap;
@@ -344,11 +465,9 @@ StepStats Engine::step() {
         a.status = misc_.p;
         a.work = nraw_.p + 1;
         a.max_probe = opts_.max_probe;
-        if (!occ)
-            occ = expand_occupancy();
         const int grid = (int)std::min<uint64_t>(n_chunks, (uint64_t)sms_ * (uint64_t)occ);
         cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
-        launch_expand(a, grid, stream_);
+        launch_expand(k64_, a, grid, stream_);
         cuda_check(cudaGetLastError(), "k_expand launch");
         cuda_check(cudaEventRecord(ev_[1], stream_), "cudaEventRecord");
         tot_.expand_launches++;
@@ -370,11 +489,12 @@ StepStats Engine::step() {
         if (!(h_status & kStatusTableOverflow))
             break;
         // Table too small for this row: clear it, grow it, redo the row.
-        cuda_check(cudaMemsetAsync(table_.p, 0, cap * sizeof(Slot), stream_), "memset table");
-        uint64_t uniq = 0;
-        for (uint32_t id : active_)
-            uniq += h_unique_[id];
-        const uint64_t want = std::max<uint64_t>(cap * 3, (uint64_t)((double)uniq * 3 / opts_.target_load));
+        cuda_check(cudaMemsetAsync(table_.p, 0, units * sizeof(ulonglong2), stream_),
+                   "memset table");
+        // Every child was produced (h_raw), so raw / load slots cannot
+        // overflow again; the memory cap applies.
+        const uint64_t want =
+            std::max<uint64_t>(cap * 8, (uint64_t)((double)h_raw / opts_.target_load));
         const uint64_t grown = table_capacity(want);
         if (grown <= cap)
             throw Error(kErrNoMem, "hash table cannot grow: device memory exhausted");
@@ -389,7 +509,9 @@ StepStats Engine::step() {
         for (uint32_t id : active_)
             uniq += h_unique_[id];
         if (uniq > opts_.max_frontier) {
-            cuda_check(cudaMemsetAsync(table_.p, 0, cap * sizeof(Slot), stream_), "memset table");
+            cuda_check(cudaMemsetAsync(table_.p, 0, cap * slot_units() * sizeof(ulonglong2),
+                                       stream_),
+                       "memset table");
             cuda_check(cudaStreamSynchronize(stream_), "memset table");
             throw Error(kErrUnsupported, "frontier limit exceeded: " + std::to_string(uniq) +
                                              " states");
@@ -416,7 +538,8 @@ StepStats Engine::step() {
     }
     const int nxt = 1 - cur_;
     keys_[nxt].reserve(std::max<uint64_t>(off, 1), stream_);
-    cnts_[nxt].reserve(std::max<uint64_t>(off, 1), stream_);
+    if (!k64_)
+        cnts_[nxt].reserve(std::max<uint64_t>(off, 1), stream_);
     cuda_check(cudaMemcpyAsync(cursor_.p, h_cursor_.data(), n_inst * sizeof(unsigned long long),
                                cudaMemcpyHostToDevice, stream_),
                "upload cursors");
@@ -425,13 +548,15 @@ StepStats Engine::step() {
     c.table = table_.p;
     c.cap = cap;
     c.cursor = cursor_.p;
-    c.out_keys = keys_[nxt].p;
+    c.out_recs = keys_[nxt].p;
     c.out_cnts = cnts_[nxt].p;
     c.results = results_.p;
     c.final_states = final_states_.p;
+    c.inst_off = inst_off_;
+    c.inst_mask = inst_mask_;
     const int cgrid = (int)std::min<uint64_t>((cap + 255) / 256, (uint64_t)sms_ * 8);
     cuda_check(cudaEventRecord(ev_[2], stream_), "cudaEventRecord");
-    launch_compact(c, cgrid, stream_);
+    launch_compact(k64_, c, cgrid, stream_);
     cuda_check(cudaGetLastError(), "k_compact launch");
     cuda_check(cudaEventRecord(ev_[3], stream_), "cudaEventRecord");
     tot_.compact_launches++;
@@ -440,14 +565,16 @@ StepStats Engine::step() {
         unsigned long long *cn = nullptr;
         const uint64_t n = std::max<uint64_t>(off, 1);
         cuda_check(cudaMalloc(&k, n * sizeof(ulonglong2)), "cudaMalloc");
-        cuda_check(cudaMalloc(&cn, n * sizeof(unsigned long long)), "cudaMalloc");
+        if (!k64_)
+            cuda_check(cudaMalloc(&cn, n * sizeof(unsigned long long)), "cudaMalloc");
         if (off) {
             cuda_check(cudaMemcpyAsync(k, keys_[nxt].p, off * sizeof(ulonglong2),
                                        cudaMemcpyDeviceToDevice, stream_),
                        "keep level");
-            cuda_check(cudaMemcpyAsync(cn, cnts_[nxt].p, off * sizeof(unsigned long long),
-                                       cudaMemcpyDeviceToDevice, stream_),
-                       "keep level");
+            if (!k64_)
+                cuda_check(cudaMemcpyAsync(cn, cnts_[nxt].p, off * sizeof(unsigned long long),
+                                           cudaMemcpyDeviceToDevice, stream_),
+                           "keep level");
         }
         lvl_keys_.push_back(k);
         lvl_cnts_.push_back(cn);
@@ -475,20 +602,28 @@ StepStats Engine::step() {
             in.active = false;
             in.done = true;
             n_active_--;
-            if (opts_.keep_levels && in.row == in.height) {
-                std::vector<unsigned long long> cn(in.seg_len);
-                if (in.seg_len)
+            unsigned long long sum = 0;
+            if (opts_.keep_levels && in.row == in.height && in.seg_len) {
+                // Final level: sum the counts of the stored states.
+                if (k64_) {
+                    std::vector<ulonglong2> rec(in.seg_len);
+                    cuda_check(cudaMemcpy(rec.data(), lvl_keys_.back(),
+                                          in.seg_len * sizeof(ulonglong2), cudaMemcpyDeviceToHost),
+                               "read final level");
+                    for (const auto &r : rec)
+                        sum += r.y;
+                } else {
+                    std::vector<unsigned long long> cn(in.seg_len);
                     cuda_check(cudaMemcpy(cn.data(), lvl_cnts_.back(),
                                           in.seg_len * sizeof(unsigned long long),
                                           cudaMemcpyDeviceToHost),
                                "read final level");
-                unsigned long long sum = 0;
-                for (auto v : cn)
-                    sum += v;
-                in.result = sum;
-            } else {
-                in.result = 0;
+                    for (auto v : cn)
+                        sum += v;
+                }
+                tot_.d2h_bytes += in.seg_len * (k64_ ? 16 : 8);
             }
+            in.result = sum;
             in.result_ready = true;
             in.seg_len = 0;
         } else {
@@ -521,35 +656,15 @@ StepStats Engine::step() {
     return st;
 }
 
-uint64_t Engine::table_capacity(uint64_t want) {
-    // At least 4096 slots, rounded to 1024; never more than the device can
-    // hold next to the frontier buffers (10% of free memory kept back).
-    want = round_up(std::max<uint64_t>(want, 4096), 1024);
-    if (want <= table_.cap)
-        return want;
-    size_t free_b = 0, total_b = 0;
-    cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
-    // Room for the next frontier (keys + counts) at the targeted load.
-    const uint64_t next_frontier =
-        (uint64_t)((double)want * opts_.target_load) * (sizeof(ulonglong2) + sizeof(unsigned long long));
-    const uint64_t avail = (uint64_t)table_.cap * sizeof(Slot) + free_b;
-    const uint64_t keep = total_b / 10 + next_frontier;
-    const uint64_t limit = avail > keep ? (avail - keep) / sizeof(Slot) : 0;
-    return std::max<uint64_t>(std::min<uint64_t>(want, limit / 1024 * 1024), 4096);
-}
-
-int Engine::expand_occupancy() {
-    int occ = 0;
-    cuda_check(expand_max_blocks_per_sm(&occ), "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-    return std::max(occ, 1);
-}
-
 uint64_t Engine::bucket_count(uint32_t id, uint32_t pattern) {
     DeviceGuard g(opts_.device);
     const Inst &in = inst_.at(id);
     if (!in.active)
         return 0;
     const unsigned long long rowmask = (1ull << in.width) - 1ull;
+    if (k64_ && in.lib.dyn_bits < in.width)
+        // Single-row pieces only: the current row is the board's, for every state.
+        return (in.desc.rows[in.row] & rowmask) == (pattern & rowmask) ? in.seg_len : 0;
     cuda_check(cudaMemsetAsync(nraw_.p, 0, sizeof(unsigned long long), stream_), "memset");
     launch_count_pattern(keys_[cur_].p + in.seg_begin, in.seg_len, rowmask, pattern & rowmask,
                          nraw_.p, sms_ * 4, stream_);
@@ -618,17 +733,20 @@ uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t
     DevBuf<unsigned long long> nsel;
     nsel.reserve(1, stream_);
     std::vector<ulonglong2 *> owned;
-    auto build_set = [&](const ulonglong2 *keys, uint64_t n) -> uint64_t {
+    auto build_set = [&](const ulonglong2 *recs, uint64_t n) -> uint64_t {
         uint64_t cap = round_up(std::max<uint64_t>(n * 2, 1024), 1024);
         for (;;) {
-            if (table_.cap < cap) {
+            const uint64_t units = cap * slot_units();
+            if (table_.cap < units) {
                 table_.release();
-                table_.reserve(cap, stream_);
+                table_clean_ = 0;
+                table_.reserve(units, stream_);
             }
-            cuda_check(cudaMemsetAsync(table_.p, 0, cap * sizeof(Slot), stream_), "memset");
+            cuda_check(cudaMemsetAsync(table_.p, 0, units * sizeof(ulonglong2), stream_),
+                       "memset");
             cuda_check(cudaMemsetAsync(misc_.p, 0, sizeof(unsigned int), stream_), "memset");
             KeySetArgs t{ table_.p, cap, misc_.p, opts_.max_probe };
-            launch_keyset_insert(t, keys, n, sms_ * 4, stream_);
+            launch_keyset_insert(k64_, t, recs, n, sms_ * 4, stream_);
             unsigned int stt = 0;
             cuda_check(cudaMemcpyAsync(&stt, misc_.p, sizeof(unsigned int), cudaMemcpyDeviceToHost,
                                        stream_),
@@ -640,14 +758,15 @@ uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t
         }
     };
     auto probe_args = [&](uint32_t r, uint64_t cap) {
+        const Seg s = seg_for(id, r);
         ProbeArgs p;
         p.insts = insts_.p;
         p.plc = plc_.p;
         p.inst = id;
         p.row = r;
-        const uint32_t R = in.desc.win_rows, W = in.width, src = r + R;
-        const unsigned long long in_row = src < H ? in.desc.rows[src] : 0u;
-        p.in_shift = in_row << ((R - 1) * W);
+        p.in_shift = s.in_shift;
+        p.hi_board = s.hi_board;
+        p.tag = s.tag;
         p.table = table_.p;
         p.cap = cap;
         p.max_probe = opts_.max_probe;
@@ -657,7 +776,8 @@ uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t
         const uint64_t cap = build_set(live[r + 1], live_n[r + 1]);
         const uint64_t n = lvl_n_[r];
         alive.reserve(std::max<uint64_t>(n, 1), stream_);
-        launch_mark_alive(probe_args((uint32_t)r, cap), lvl_keys_[r], n, alive.p, sms_ * 4, stream_);
+        launch_mark_alive(k64_, probe_args((uint32_t)r, cap), lvl_keys_[r], n, alive.p, sms_ * 4,
+                          stream_);
         ulonglong2 *out = nullptr;
         cuda_check(cudaMalloc(&out, std::max<uint64_t>(n, 1) * sizeof(ulonglong2)), "cudaMalloc");
         owned.push_back(out);
@@ -679,7 +799,7 @@ uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t
         ulonglong2 rk;
         cuda_check(cudaMemcpy(&rk, lvl_keys_[0], sizeof(rk), cudaMemcpyDeviceToHost), "read root");
         root.k0 = rk.x;
-        root.k1 = rk.y;
+        root.k1 = k64_ ? 0ull : rk.y;
         root.parent = ~0u;
         root.nfill = 0;
     }
@@ -696,7 +816,7 @@ uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t
                                    cudaMemcpyHostToDevice, stream_),
                    "upload nodes");
         cuda_check(cudaMemsetAsync(dn.p, 0, 2 * sizeof(unsigned int), stream_), "memset");
-        launch_extend_paths(probe_args(r, cap), din.p, n, dout.p, dn.p, max_nodes, dn.p + 1,
+        launch_extend_paths(k64_, probe_args(r, cap), din.p, n, dout.p, dn.p, max_nodes, dn.p + 1,
                             sms_ * 4, stream_);
         unsigned int hn[2] = {0, 0};
         cuda_check(cudaMemcpyAsync(hn, dn.p, sizeof(hn), cudaMemcpyDeviceToHost, stream_),
@@ -711,6 +831,7 @@ uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t
     }
     for (auto p : owned)
         cudaFree(p);
+    table_clean_ = 0;   // the table now holds membership sets
 
     // Leaves -> grids.  Steps are numbered in anchor order (row-major), the
     // order in which the reference's solver places them.

@@ -57,13 +57,16 @@ struct DevBuf {
     void reserve(size_t n, cudaStream_t s, size_t keep = 0);
 };
 
+enum class KeyMode { Auto, K64, K128 };
+
 struct EngineOpts {
     int device = 0;
     uint32_t max_probe = 512;
     bool keep_levels = false;      // retain every level (needed for solutions; one instance)
     double target_load = 0.5;      // hash table load factor aimed at when sizing
-    uint64_t chunk_states = 1024;  // frontier states per CTA work item
+    uint64_t chunk_states = 4096;  // largest number of frontier states per CTA work item
     uint64_t max_frontier = 0;     // abort when a row yields more states (0 = no limit)
+    KeyMode key_mode = KeyMode::Auto;  // Auto: K64 when every instance's packed key fits
 };
 
 struct InstanceSpec {
@@ -100,8 +103,8 @@ public:
     Engine(const Engine &) = delete;
     Engine &operator=(const Engine &) = delete;
 
-    // Adds an instance (validated, tables uploaded); its root state joins the
-    // frontier at the next step().  Returns the instance id.
+    // Adds an instance (validated); its tables are uploaded and its root
+    // state joins the frontier at the next step().  Returns the instance id.
     uint32_t add(const InstanceSpec &spec);
 
     // Advances every active instance by one row.
@@ -131,6 +134,7 @@ public:
 
     const Totals &totals() const { return tot_; }
     void set_max_frontier(uint64_t n) { opts_.max_frontier = n; }
+    bool packed_keys() const { return k64_; }
     cudaStream_t stream() const { return stream_; }
     int sm_count() const { return sms_; }
 
@@ -144,19 +148,30 @@ private:
         uint64_t seg_begin = 0, seg_len = 0;
         uint64_t result = 0;
         std::vector<uint64_t> level_sizes;
-        unsigned long long root_k0 = 0, root_k1 = 0;
+        unsigned long long root_window = 0;
     };
 
     void ensure_inst_capacity(size_t n);
+    void fix_key_mode();
     void flush_uploads();
     int expand_occupancy();
     uint64_t table_capacity(uint64_t want);
+    size_t slot_units() const { return k64_ ? 1 : 2; }   // table slot size in 16-byte units
+    Seg seg_for(uint32_t id, uint32_t row) const;
+    ulonglong2 root_record(uint32_t id) const;
 
     EngineOpts opts_;
     int sms_ = 0;
+    int occ64_ = 0, occ128_ = 0;   // resident k_expand CTAs per SM
     cudaStream_t stream_ = nullptr;
     cudaEvent_t ev_[4] = {};
     cudaEvent_t ev_run_[2] = {};
+
+    // Key encoding, fixed at the first step.
+    bool mode_fixed_ = false;
+    bool k64_ = false;
+    uint32_t inst_off_ = 0;           // K64: instance id position
+    unsigned long long inst_mask_ = 0;
 
     std::vector<Inst> inst_;
     std::vector<uint32_t> pending_;          // roots not yet in the frontier
@@ -172,17 +187,18 @@ private:
     DevBuf<unsigned long long> cursor_;
     DevBuf<unsigned long long> results_;
     DevBuf<unsigned int> final_states_;
-    DevBuf<unsigned int> misc_;   // [0] status, [1] work counter
-    DevBuf<unsigned long long> nraw_;
+    DevBuf<unsigned int> misc_;   // [0] status
+    DevBuf<unsigned long long> nraw_;  // [0] raw children, [1] chunk work counter
     DevBuf<Seg> segs_;
 
+    // Frontier (ping-pong): K64 {key, count} records, or K128 keys + counts.
     DevBuf<ulonglong2> keys_[2];
     DevBuf<unsigned long long> cnts_[2];
     int cur_ = 0;
     uint64_t n_cur_ = 0;
 
-    DevBuf<Slot> table_;
-    uint64_t table_clean_ = 0;    // slots [0, table_clean_) are known to be zero
+    DevBuf<ulonglong2> table_;    // slot_units() 16-byte units per slot
+    uint64_t table_clean_ = 0;    // units [0, table_clean_) are known to be zero
     double growth_ = 8.0;
 
     // keep_levels storage: level r = states after completing r rows (r = 0 is the root).

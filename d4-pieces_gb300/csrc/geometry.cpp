@@ -148,6 +148,8 @@ std::string build_piece_lib(const uint64_t *shapes, const uint32_t *counts, uint
     out.sym = sym & 0xFFu;
     out.width = width;
     out.win_rows = 64 / width;
+    if (n > (uint32_t)kMaxTypes)
+        return "more than 40 piece types";
     uint32_t base = 0;
     for (uint32_t i = 0; i < n; i++) {
         if (!shapes[i])
@@ -157,12 +159,22 @@ std::string build_piece_lib(const uint64_t *shapes, const uint32_t *counts, uint
         out.shapes.push_back(shapes[i]);
         out.counts.push_back(counts[i]);
         const uint32_t c = counts[i];
-        if (base + c > (uint32_t)kMaxCopies)
-            return "more than 40 piece copies";
-        out.type_mask.push_back(c ? (((1ull << c) - 1) << base) : 0ull);
-        base += c;
+        // binary counter of bit_length(c) bits (none for an absent type)
+        uint32_t bits = 0;
+        while (bits < 32 && (c >> bits))
+            bits++;
+        if (base + bits > (uint32_t)kMaxUsedBits)
+            return "more than 40 bits of piece copy counters";
+        TypeField tf{};
+        if (bits) {
+            tf.fm = ((1ull << bits) - 1) << base;
+            tf.cap = (unsigned long long)c << base;
+        }
+        out.fields.push_back(tf);
+        out.copies += c;
+        base += bits;
     }
-    out.copies = base;
+    out.used_bits = base;
 
     // Distinct allowed orientations per type, in Shape::transforms() order
     // (the enabled placements of Piece::Piece, src/Piece.cpp:12-22).
@@ -172,6 +184,8 @@ std::string build_piece_lib(const uint64_t *shapes, const uint32_t *counts, uint
     };
     std::vector<Orient> orients;
     for (uint32_t i = 0; i < n; i++) {
+        if (!counts[i])
+            continue;
         std::vector<uint64_t> seen;
         unsigned s = out.sym;
         for (int t = 0; t < 8; t++, s >>= 1) {
@@ -198,6 +212,7 @@ std::string build_piece_lib(const uint64_t *shapes, const uint32_t *counts, uint
     }
     if (out.max_piece_rows > out.win_rows)
         return "piece taller than the row window of this board width";
+    out.dyn_bits = out.max_piece_rows ? width * (out.max_piece_rows - 1) : 0;
 
     // Placements anchored at each column: the anchor is the piece's first
     // cell in row-major order (the lowest set bit), which the row-by-row
@@ -213,7 +228,7 @@ std::string build_piece_lib(const uint64_t *shapes, const uint32_t *counts, uint
             uint64_t m = 0;
             for (int k = 0; k < o.ncells; k++)
                 m |= 1ull << (o.cr[k] * (int)width + o.cc[k] + x);
-            out.plc.push_back(Plc{ m, out.type_mask[o.type] });
+            out.plc.push_back(Plc{ m, o.type, 0u });
             out.plc_type.push_back((uint16_t)o.type);
             out.plc_orient.push_back(o.t);
         }

@@ -37,7 +37,9 @@ struct PieceLib {
     uint32_t win_rows = 8;          // 64 / width
     uint32_t copies = 0;            // sum of counts
     uint32_t max_piece_rows = 0;
-    std::vector<uint64_t> type_mask;     // copy bits per type
+    uint32_t used_bits = 0;         // bits of the per-type binary copy counters
+    uint32_t dyn_bits = 0;          // width * (max_piece_rows - 1)
+    std::vector<TypeField> fields;       // copy counter per type
     std::vector<Plc> plc;                // grouped by anchor column
     std::vector<uint16_t> plc_type;      // type id per placement
     std::vector<uint32_t> plc_orient;    // transform index per placement

@@ -5,13 +5,15 @@
 //               + impl<H> (src/kernel.cuh:12-227).  Each state is expanded by
 //               every whole-row fill -- a depth-first walk over placements
 //               anchored at the lowest empty cell of the current row, with
-//               the placement table staged in shared memory -- and each child
-//               is inserted straight into an HBM-resident open-addressing
-//               table (128-bit key CAS + 64-bit count add), which replaces
-//               the reference's ring buffer + host hash-set Sorter
+//               the instance's placement table staged in shared memory -- and
+//               each child is inserted straight into an HBM-resident
+//               open-addressing table (key CAS + 64-bit count add), which
+//               replaces the reference's ring buffer + host hash-set Sorter
 //               (src/device.cu:14-309, src/sorter.cpp:72-214).
 //   k_compact : moves the table into the next frontier, instance by
 //               instance, clearing it for the next row.
+// Both are templated on the key encoding (K64 packed / K128 general, see
+// d4e_types.h).
 #include "kernels.h"
 
 #include <cuda_runtime.h>
@@ -32,8 +34,18 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
     return x;
 }
 
-__device__ __forceinline__ unsigned long long hash_key(unsigned long long k0, unsigned long long k1) {
-    return mix64(k0 ^ mix64(k1 ^ 0x9e3779b97f4a7c15ull));
+// Home slot in a table of `cap` slots (any capacity): the high half of
+// hash * cap maps the 64-bit hash uniformly onto [0, cap).
+__device__ __forceinline__ unsigned long long home64(unsigned long long key, unsigned long long cap) {
+    return __umul64hi(mix64(key), cap);
+}
+__device__ __forceinline__ unsigned long long home128(unsigned long long k0, unsigned long long k1,
+                                                      unsigned long long cap) {
+    return __umul64hi(mix64(k0 ^ mix64(k1 ^ 0x9e3779b97f4a7c15ull)), cap);
+}
+
+__device__ __forceinline__ unsigned long long next_slot(unsigned long long h, unsigned long long cap) {
+    return h + 1 == cap ? 0ull : h + 1;
 }
 
 // 128-bit compare-and-swap on a 16-byte aligned global address (sm_90+).
@@ -52,20 +64,36 @@ __device__ __forceinline__ void cas128(unsigned long long *addr,
         : "memory");
 }
 
-// Home slot of a key in a table of `cap` slots (any capacity): the high
-// half of hash * cap maps the 64-bit hash uniformly onto [0, cap).
-__device__ __forceinline__ unsigned long long home_slot(unsigned long long k0, unsigned long long k1,
-                                                        unsigned long long cap) {
-    return __umul64hi(hash_key(k0, k1), cap);
+// Insert with multiplicity cnt (linear probing).  Returns 1 for a newly
+// claimed key, 0 for an existing one, -1 when the probe limit was reached.
+__device__ __forceinline__ int insert64(Slot16 *__restrict__ T, unsigned long long cap,
+                                        unsigned long long key, unsigned long long cnt,
+                                        unsigned int max_probe) {
+    unsigned long long h = home64(key, cap);
+    for (unsigned int p = 0; p < max_probe; ++p) {
+        // A naturally aligned 8-byte load is single-copy atomic: a key seen
+        // here is final.  Only an empty slot needs the CAS.
+        unsigned long long k = __ldcg(&T[h].key);
+        if (k == 0ull) {
+            k = atomicCAS(&T[h].key, 0ull, key);
+            if (k == 0ull) {
+                atomicAdd(&T[h].cnt, cnt);
+                return 1;
+            }
+        }
+        if (k == key) {
+            atomicAdd(&T[h].cnt, cnt);
+            return 0;
+        }
+        h = next_slot(h, cap);
+    }
+    return -1;
 }
 
-// Insert (k0, k1) with multiplicity cnt (linear probing).  Returns 1 for a
-// newly claimed key, 0 for an existing one, -1 when the probe limit was
-// reached.
-__device__ __forceinline__ int table_insert(Slot *__restrict__ T, unsigned long long cap,
-                                            unsigned long long k0, unsigned long long k1,
-                                            unsigned long long cnt, unsigned int max_probe) {
-    unsigned long long h = home_slot(k0, k1, cap);
+__device__ __forceinline__ int insert128(Slot32 *__restrict__ T, unsigned long long cap,
+                                         unsigned long long k0, unsigned long long k1,
+                                         unsigned long long cnt, unsigned int max_probe) {
+    unsigned long long h = home128(k0, k1, cap);
     for (unsigned int p = 0; p < max_probe; ++p) {
         unsigned long long o0, o1;
         cas128(&T[h].k0, 0ull, 0ull, k0, k1, o0, o1);
@@ -74,54 +102,82 @@ __device__ __forceinline__ int table_insert(Slot *__restrict__ T, unsigned long 
             atomicAdd(&T[h].cnt, cnt);
             return claimed ? 1 : 0;
         }
-        h = h + 1 == cap ? 0ull : h + 1;
+        h = next_slot(h, cap);
     }
     return -1;
 }
 
-__device__ __forceinline__ bool table_find(const Slot *__restrict__ T, unsigned long long cap,
-                                           unsigned long long k0, unsigned long long k1,
-                                           unsigned int max_probe) {
-    unsigned long long h = home_slot(k0, k1, cap);
+// Membership lookups (the table is read-only while they run).
+__device__ __forceinline__ bool find64(const Slot16 *__restrict__ T, unsigned long long cap,
+                                       unsigned long long key, unsigned int max_probe) {
+    unsigned long long h = home64(key, cap);
+    for (unsigned int p = 0; p < max_probe; ++p) {
+        const unsigned long long k = T[h].key;
+        if (k == key)
+            return true;
+        if (k == 0ull)
+            return false;
+        h = next_slot(h, cap);
+    }
+    return false;
+}
+
+__device__ __forceinline__ bool find128(const Slot32 *__restrict__ T, unsigned long long cap,
+                                        unsigned long long k0, unsigned long long k1,
+                                        unsigned int max_probe) {
+    unsigned long long h = home128(k0, k1, cap);
     for (unsigned int p = 0; p < max_probe; ++p) {
         const ulonglong2 k = *reinterpret_cast<const ulonglong2 *>(&T[h].k0);
         if (k.x == k0 && k.y == k1)
             return true;
         if ((k.x | k.y) == 0ull)
             return false;
-        h = h + 1 == cap ? 0ull : h + 1;
+        h = next_slot(h, cap);
     }
     return false;
 }
 
 // Shared-memory copy of one instance's placement table.
 struct SmemTable {
-    Plc plc[kMaxPlc];
+    unsigned long long mask[kMaxPlc];
+    uint8_t type[kMaxPlc];
+    TypeField field[kMaxTypes];
     uint16_t off[kMaxWidth];
     uint16_t len[kMaxWidth];
     uint32_t width;
+    uint32_t dyn_bits;
+    uint32_t used_bits;
 };
 
 __device__ __forceinline__ void load_table(SmemTable &st, const InstDesc *__restrict__ d,
                                            const Plc *__restrict__ plc_all) {
     const uint32_t np = d->n_plc;
     const Plc *src = plc_all + d->plc_off;
-    for (uint32_t i = threadIdx.x; i < np; i += blockDim.x)
-        st.plc[i] = src[i];
+    for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) {
+        const Plc p = src[i];
+        st.mask[i] = p.mask;
+        st.type[i] = (uint8_t)p.type;
+    }
+    for (uint32_t i = threadIdx.x; i < d->n_types; i += blockDim.x)
+        st.field[i] = d->types[i];
     if (threadIdx.x < kMaxWidth) {
         st.off[threadIdx.x] = d->col_off[threadIdx.x];
         st.len[threadIdx.x] = d->col_len[threadIdx.x];
     }
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0) {
         st.width = d->width;
+        st.dyn_bits = d->dyn_bits;
+        st.used_bits = d->used_bits;
+    }
 }
 
-// Depth-first enumeration of the whole-row fills of one state.  The fill
-// stack lives in two registers: 8-bit placement index and 4-bit anchor
-// column per depth (a row of <= 8 cells takes <= 8 placements).  A placement
-// is undone by restoring its cells and dropping the highest used copy bit of
-// its type.  `emit(child_window, used, sidx, scol, depth)` is called at every
-// completed row; returning true stops the walk.
+// Depth-first enumeration of the whole-row fills of one state (window w,
+// copy counters u).  The fill stack lives in two registers: 8-bit placement
+// index and 4-bit anchor column per depth (a row of <= 8 cells takes <= 8
+// placements).  A placement is undone by restoring its cells and decrementing
+// its type's counter.  `emit(window, used, sidx, scol, depth)` is called at
+// every completed row with the window before the shift; returning true stops
+// the walk.
 template <class Emit>
 __device__ __forceinline__ void row_fills(const SmemTable &st, unsigned long long w,
                                           unsigned long long u, Emit &&emit) {
@@ -133,24 +189,23 @@ __device__ __forceinline__ void row_fills(const SmemTable &st, unsigned long lon
         const uint32_t row = (uint32_t)w & rowmask;
         bool down = false;
         if (row == 0) {
-            if (emit(w >> W, u, sidx, scol, depth))
+            if (emit(w, u, sidx, scol, depth))
                 return;
         } else {
             const uint32_t c = __ffs(row) - 1;
             const uint32_t off = st.off[c], len = st.len[c];
             for (; idx < len; ++idx) {
-                const Plc p = st.plc[off + idx];
-                if (p.mask & ~w)
+                const unsigned long long m = st.mask[off + idx];
+                if (m & ~w)
                     continue;
-                const unsigned long long ut = u & p.tm;
-                const unsigned long long nb = (ut + (p.tm & (0ull - p.tm))) & p.tm;
-                if (!nb)
+                const TypeField f = st.field[st.type[off + idx]];
+                if ((u & f.fm) >= f.cap)
                     continue;
                 sidx |= (unsigned long long)idx << (8 * depth);
                 scol |= c << (4 * depth);
                 ++depth;
-                w &= ~p.mask;
-                u |= nb;
+                w &= ~m;
+                u += f.fm & (0ull - f.fm);
                 idx = 0;
                 down = true;
                 break;
@@ -165,27 +220,111 @@ __device__ __forceinline__ void row_fills(const SmemTable &st, unsigned long lon
         sidx &= ~(0xFFull << (8 * depth));
         const uint32_t c = (scol >> (4 * depth)) & 0xFu;
         scol &= ~(0xFu << (4 * depth));
-        const Plc p = st.plc[st.off[c] + idx];
-        w |= p.mask;
-        const unsigned long long ut = u & p.tm;
-        u &= ~(ut & ~(ut >> 1));
+        const uint32_t pi = st.off[c] + idx;
+        w |= st.mask[pi];
+        const unsigned long long fm = st.field[st.type[pi]].fm;
+        u -= fm & (0ull - fm);
         ++idx;
     }
 }
 
+// Key codec -----------------------------------------------------------------
+struct Codec {
+    unsigned long long dynmask, usedmask, hi_board, in_shift, tag;
+    uint32_t W, dyn_bits;
+
+    // K64: window = kept rows | board rows below them; used above the window.
+    __device__ __forceinline__ void parse64(unsigned long long key, unsigned long long &w,
+                                            unsigned long long &u) const {
+        w = (key & dynmask) | hi_board;
+        u = (key >> dyn_bits) & usedmask;
+    }
+    __device__ __forceinline__ unsigned long long child64(unsigned long long w,
+                                                          unsigned long long u) const {
+        return ((w >> W) & dynmask) | (u << dyn_bits) | tag;
+    }
+};
+
+__device__ __forceinline__ Codec make_codec(const SmemTable &st, unsigned long long hi_board,
+                                            unsigned long long in_shift, unsigned long long tag) {
+    Codec c;
+    c.W = st.width;
+    c.dyn_bits = st.dyn_bits;
+    c.dynmask = (1ull << st.dyn_bits) - 1ull;
+    c.usedmask = (1ull << st.used_bits) - 1ull;
+    c.hi_board = hi_board;
+    c.in_shift = in_shift;
+    c.tag = tag;
+    return c;
+}
+
+template <bool K64>
+__device__ __forceinline__ void parse_key(const Codec &cd, unsigned long long k0,
+                                          unsigned long long k1, unsigned long long &w,
+                                          unsigned long long &u) {
+    if constexpr (K64) {
+        cd.parse64(k0, w, u);
+    } else {
+        w = k0;
+        u = k1 & kUsedMask128;
+    }
+}
+
+// Children staged per warp before the warp inserts them together.
+constexpr int kWarps = kExpandBlock / 32;
+constexpr int kStage = 64;
+struct WarpStage {
+    unsigned long long k0[kStage];
+    unsigned long long k1[kStage];
+    unsigned long long cnt[kStage];
+};
+
+template <bool K64>
+__device__ __forceinline__ void flush_children(const ExpandArgs &a, const WarpStage &ws, int base,
+                                               int n, uint32_t inst, unsigned lane) {
+    // Lane i inserts child base + i: up to 32 independent inserts in flight.
+    int r = 2;
+    if ((int)lane < n) {
+        const int j = base + (int)lane;
+        if constexpr (K64)
+            r = insert64(static_cast<Slot16 *>(a.table), a.cap, ws.k0[j], ws.cnt[j], a.max_probe);
+        else
+            r = insert128(static_cast<Slot32 *>(a.table), a.cap, ws.k0[j], ws.k1[j], ws.cnt[j],
+                          a.max_probe);
+    }
+    const unsigned fresh = __ballot_sync(0xffffffffu, r == 1);
+    if (__any_sync(0xffffffffu, r < 0) && lane == 0)
+        atomicOr(a.status, kStatusTableOverflow);
+    if (fresh && lane == 0)
+        atomicAdd(&a.inst_unique[inst], (unsigned)__popc(fresh));
+}
+
+// Expansion.  Every iteration of the warp loop performs exactly one step of
+// each lane's depth-first walk -- test one candidate placement, descend,
+// backtrack, or complete the row -- so the lanes of a warp do uniform work;
+// a lane whose state is exhausted takes the next state of the CTA's chunk.
+// Completed rows are staged in shared memory and inserted by the whole warp,
+// 32 at a time.
+template <bool K64>
 __global__ void __launch_bounds__(kExpandBlock)
 k_expand(ExpandArgs a) {
     __shared__ SmemTable st;
+    __shared__ WarpStage stage[kWarps];
     __shared__ Seg s_seg;
     __shared__ unsigned long long s_ci;
+    __shared__ unsigned int s_next;
     uint32_t loaded = 0xFFFFFFFFu;
     unsigned long long raw = 0;
     const unsigned lane = threadIdx.x & 31u;
+    const unsigned warp = threadIdx.x >> 5;
+    WarpStage &ws = stage[warp];
+    const unsigned lt_mask = (1u << lane) - 1u;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) {
             const unsigned long long ci = atomicAdd(a.work, 1ull);
             s_ci = ci;
+            s_next = 0;
             if (ci < a.n_chunks) {
                 // Segment holding chunk ci: last seg with chunk_base <= ci.
                 uint32_t lo = 0, hi = a.n_segs - 1;
@@ -211,29 +350,146 @@ k_expand(ExpandArgs a) {
         }
         const unsigned long long first = sg.begin + (ci - sg.chunk_base) * a.chunk_states;
         const unsigned long long segend = sg.begin + sg.len;
-        const unsigned long long last =
-            first + a.chunk_states < segend ? first + a.chunk_states : segend;
-        const unsigned long long in_shift = sg.in_shift;
+        const unsigned n_items = (unsigned)((first + a.chunk_states < segend ? first + a.chunk_states
+                                                                             : segend) -
+                                            first);
+        const uint32_t fan = a.fan;
+        const Codec cd = make_codec(st, sg.hi_board, sg.in_shift, sg.tag);
         const uint32_t inst = sg.inst;
-        for (unsigned long long s = first + threadIdx.x; s < last; s += blockDim.x) {
-            const ulonglong2 key = a.keys[s];
-            const unsigned long long cnt = a.cnts[s];
-            row_fills(st, key.x, key.y,
-                      [&](unsigned long long cw, unsigned long long u, unsigned long long,
-                          uint32_t, uint32_t) {
-                          ++raw;
-                          const int r = table_insert(a.table, a.cap, cw | in_shift, u, cnt,
-                                                     a.max_probe);
-                          if (r < 0)
-                              atomicOr(a.status, kStatusTableOverflow);
-                          // All lanes of a warp work on the same chunk, hence the
-                          // same instance: aggregate the new-key count per warp.
-                          const unsigned act = __activemask();
-                          const unsigned fresh = __ballot_sync(act, r == 1);
-                          if (fresh && lane == (unsigned)(__ffs(fresh) - 1))
-                              atomicAdd(&a.inst_unique[inst], (unsigned)__popc(fresh));
-                          return false;
-                      });
+        const uint32_t W = st.width;
+        const uint32_t rowmask = (1u << W) - 1u;
+
+        // Lane walk state.
+        bool active = false, exhausted = false;
+        unsigned long long w = 0, u = 0, cnt = 0, sidx = 0;
+        uint32_t scol = 0, depth = 0, idx = 0, min_depth = 0;
+        int nbuf = 0;   // warp-uniform: staged children
+        for (;;) {
+            if (!active && !exhausted) {
+                const unsigned i = atomicAdd(&s_next, 1u);
+                if (i < n_items) {
+                    const unsigned long long item = first + i;
+                    const unsigned long long si = fan ? item / fan : item;
+                    const ulonglong2 rec = a.recs[si];
+                    parse_key<K64>(cd, rec.x, rec.y, w, u);
+                    cnt = K64 ? rec.y : a.cnts[si];
+                    sidx = 0;
+                    scol = 0;
+                    depth = 0;
+                    idx = 0;
+                    active = true;
+                    if (fan) {
+                        // Split walk: place this item's first choice at the
+                        // root, then walk only beneath it (min_depth = 1).
+                        const uint32_t choice = (uint32_t)(item % fan);
+                        const uint32_t row = (uint32_t)w & rowmask;
+                        if (row == 0) {
+                            active = choice == 0;   // complete row: one item emits it
+                            min_depth = 0;
+                        } else {
+                            const uint32_t c = __ffs(row) - 1;
+                            active = false;
+                            if (choice < st.len[c]) {
+                                const uint32_t pi = st.off[c] + choice;
+                                const unsigned long long m = st.mask[pi];
+                                if (!(m & ~w)) {
+                                    const TypeField f = st.field[st.type[pi]];
+                                    if ((u & f.fm) < f.cap) {
+                                        sidx = choice;
+                                        scol = c;
+                                        depth = 1;
+                                        w &= ~m;
+                                        u += f.fm & (0ull - f.fm);
+                                        active = true;
+                                        min_depth = 1;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                } else {
+                    exhausted = true;
+                }
+            }
+            bool emit = false, pop = false;
+            unsigned long long ck0 = 0, ck1 = 0;
+            if (active) {
+                const uint32_t row = (uint32_t)w & rowmask;
+                if (row == 0) {
+                    // Row complete: the child, then back to the parent fill.
+                    emit = true;
+                    if constexpr (K64) {
+                        ck0 = cd.child64(w, u);
+                    } else {
+                        ck0 = (w >> W) | cd.in_shift;
+                        ck1 = u | cd.tag;
+                    }
+                    pop = true;
+                } else {
+                    const uint32_t c = __ffs(row) - 1;
+                    if (idx < st.len[c]) {
+                        const uint32_t pi = st.off[c] + idx;
+                        const unsigned long long m = st.mask[pi];
+                        bool take = !(m & ~w);
+                        TypeField f;
+                        if (take) {
+                            f = st.field[st.type[pi]];
+                            take = (u & f.fm) < f.cap;
+                        }
+                        if (take) {
+                            sidx |= (unsigned long long)idx << (8 * depth);
+                            scol |= c << (4 * depth);
+                            ++depth;
+                            w &= ~m;
+                            u += f.fm & (0ull - f.fm);
+                            idx = 0;
+                        } else {
+                            ++idx;
+                        }
+                    } else {
+                        pop = true;
+                    }
+                }
+                if (pop) {
+                    if (depth == min_depth) {
+                        active = false;
+                    } else {
+                        --depth;
+                        idx = (uint32_t)(sidx >> (8 * depth)) & 0xFFu;
+                        sidx &= ~(0xFFull << (8 * depth));
+                        const uint32_t c = (scol >> (4 * depth)) & 0xFu;
+                        scol &= ~(0xFu << (4 * depth));
+                        const uint32_t pi = st.off[c] + idx;
+                        w |= st.mask[pi];
+                        const unsigned long long fm = st.field[st.type[pi]].fm;
+                        u -= fm & (0ull - fm);
+                        ++idx;
+                    }
+                }
+            }
+            // Stage this iteration's children (<= 32) after the staged ones.
+            const unsigned em = __ballot_sync(0xffffffffu, emit);
+            if (emit) {
+                const int pos = nbuf + __popc(em & lt_mask);
+                ws.k0[pos] = ck0;
+                ws.k1[pos] = ck1;
+                ws.cnt[pos] = cnt;
+                ++raw;
+            }
+            nbuf += __popc(em);
+            if (nbuf >= 32) {
+                __syncwarp();
+                flush_children<K64>(a, ws, nbuf - 32, 32, inst, lane);
+                nbuf -= 32;
+                __syncwarp();
+            }
+            if (__all_sync(0xffffffffu, !active && exhausted))
+                break;
+        }
+        if (nbuf > 0) {
+            __syncwarp();
+            flush_children<K64>(a, ws, 0, nbuf, inst, lane);
+            __syncwarp();
         }
     }
     // Reconverged here: one atomic per warp for the raw-children counter.
@@ -244,6 +500,7 @@ k_expand(ExpandArgs a) {
         atomicAdd(a.n_raw, tot);
 }
 
+template <bool K64>
 __global__ void __launch_bounds__(kCompactBlock)
 k_compact(CompactArgs a) {
     const unsigned lane = threadIdx.x & 31u;
@@ -251,16 +508,28 @@ k_compact(CompactArgs a) {
     for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < a.cap;
          base += stride) {
         const unsigned long long i = base + threadIdx.x;
-        Slot s{0, 0, 0, 0};
+        unsigned long long k0 = 0, k1 = 0, cnt = 0;
+        bool occ = false;
+        uint32_t inst = 0xFFFFFFFFu;
         if (i < a.cap) {
-            const ulonglong4_32a v = *reinterpret_cast<const ulonglong4_32a *>(&a.table[i]);
-            s.k0 = v.x;
-            s.k1 = v.y;
-            s.cnt = v.z;
+            if constexpr (K64) {
+                const ulonglong2 v = static_cast<const ulonglong2 *>(a.table)[i];
+                k0 = v.x;
+                cnt = v.y;
+                occ = k0 != 0ull;
+                if (occ)
+                    inst = (uint32_t)((k0 >> a.inst_off) & a.inst_mask);
+            } else {
+                const ulonglong4_32a v = static_cast<const ulonglong4_32a *>(a.table)[i];
+                k0 = v.x;
+                k1 = v.y;
+                cnt = v.z;
+                occ = k1 != 0ull;
+                if (occ)
+                    inst = (uint32_t)((k1 & ~kMarker) >> kInstShift128);
+            }
         }
-        const bool occ = s.k1 != 0ull;
-        const uint32_t inst = occ ? (uint32_t)((s.k1 & ~kMarker) >> kInstShift) : 0xFFFFFFFFu;
-        unsigned long long cur = occ ? a.cursor[inst] : 0ull;
+        const unsigned long long cur = occ ? a.cursor[inst] : 0ull;
         const bool fin = occ && cur == kCursorFinal;
         const bool store = occ && !fin;
         // Warp-aggregated cursor bump per instance.
@@ -272,50 +541,85 @@ k_compact(CompactArgs a) {
                 basepos = atomicAdd(&a.cursor[inst], (unsigned long long)__popc(peers));
             basepos = __shfl_sync(peers, basepos, leader);
             const unsigned long long pos = basepos + __popc(peers & ((1u << lane) - 1u));
-            a.out_keys[pos] = make_ulonglong2(s.k0, s.k1);
-            a.out_cnts[pos] = s.cnt;
+            if constexpr (K64) {
+                a.out_recs[pos] = make_ulonglong2(k0, cnt);
+            } else {
+                a.out_recs[pos] = make_ulonglong2(k0, k1);
+                a.out_cnts[pos] = cnt;
+            }
         }
         if (fin) {
-            atomicAdd(&a.results[inst], s.cnt);
+            atomicAdd(&a.results[inst], cnt);
             atomicAdd(&a.final_states[inst], 1u);
         }
-        if (occ)
-            *reinterpret_cast<ulonglong4_32a *>(&a.table[i]) = make_ulonglong4_32a(0, 0, 0, 0);
+        if (occ) {
+            if constexpr (K64)
+                static_cast<ulonglong2 *>(a.table)[i] = make_ulonglong2(0, 0);
+            else
+                static_cast<ulonglong4_32a *>(a.table)[i] = make_ulonglong4_32a(0, 0, 0, 0);
+        }
     }
 }
 
-__global__ void k_keyset_insert(KeySetArgs t, const ulonglong2 *__restrict__ keys,
+template <bool K64>
+__global__ void k_keyset_insert(KeySetArgs t, const ulonglong2 *__restrict__ recs,
                                 unsigned long long n) {
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += stride) {
-        const ulonglong2 k = keys[i];
-        if (table_insert(t.table, t.cap, k.x, k.y, 0ull, t.max_probe) < 0)
+        const ulonglong2 k = recs[i];
+        int r;
+        if constexpr (K64)
+            r = insert64(static_cast<Slot16 *>(t.table), t.cap, k.x, 0ull, t.max_probe);
+        else
+            r = insert128(static_cast<Slot32 *>(t.table), t.cap, k.x, k.y, 0ull, t.max_probe);
+        if (r < 0)
             atomicOr(t.status, kStatusTableOverflow);
     }
 }
 
+template <bool K64>
+__device__ __forceinline__ bool probe_child(const ProbeArgs &p, const Codec &cd,
+                                            unsigned long long wd, unsigned long long ud,
+                                            unsigned long long &ck0, unsigned long long &ck1) {
+    if constexpr (K64) {
+        ck0 = cd.child64(wd, ud);
+        ck1 = 0ull;
+        return find64(static_cast<const Slot16 *>(p.table), p.cap, ck0, p.max_probe);
+    } else {
+        ck0 = (wd >> cd.W) | cd.in_shift;
+        ck1 = ud | cd.tag;
+        return find128(static_cast<const Slot32 *>(p.table), p.cap, ck0, ck1, p.max_probe);
+    }
+}
+
+template <bool K64>
 __global__ void __launch_bounds__(kExpandBlock)
-k_mark_alive(ProbeArgs p, const ulonglong2 *__restrict__ keys, unsigned long long n,
+k_mark_alive(ProbeArgs p, const ulonglong2 *__restrict__ recs, unsigned long long n,
              unsigned char *__restrict__ alive) {
     __shared__ SmemTable st;
     load_table(st, p.insts + p.inst, p.plc);
     __syncthreads();
+    const Codec cd = make_codec(st, p.hi_board, p.in_shift, p.tag);
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += stride) {
-        const ulonglong2 k = keys[i];
+        const ulonglong2 k = recs[i];
+        unsigned long long w, u;
+        parse_key<K64>(cd, k.x, k.y, w, u);
         bool found = false;
-        row_fills(st, k.x, k.y,
-                  [&](unsigned long long cw, unsigned long long u, unsigned long long, uint32_t,
+        row_fills(st, w, u,
+                  [&](unsigned long long wd, unsigned long long ud, unsigned long long, uint32_t,
                       uint32_t) {
-                      found = table_find(p.table, p.cap, cw | p.in_shift, u, p.max_probe);
+                      unsigned long long a, b;
+                      found = probe_child<K64>(p, cd, wd, ud, a, b);
                       return found;
                   });
         alive[i] = found ? 1 : 0;
     }
 }
 
+template <bool K64>
 __global__ void __launch_bounds__(kExpandBlock)
 k_extend_paths(ProbeArgs p, const PathNode *__restrict__ nodes, uint32_t n_nodes,
                PathNode *__restrict__ out, unsigned int *__restrict__ n_out, uint32_t max_out,
@@ -323,14 +627,17 @@ k_extend_paths(ProbeArgs p, const PathNode *__restrict__ nodes, uint32_t n_nodes
     __shared__ SmemTable st;
     load_table(st, p.insts + p.inst, p.plc);
     __syncthreads();
+    const Codec cd = make_codec(st, p.hi_board, p.in_shift, p.tag);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_nodes;
          i += gridDim.x * blockDim.x) {
         const PathNode nd = nodes[i];
-        row_fills(st, nd.k0, nd.k1,
-                  [&](unsigned long long cw, unsigned long long u, unsigned long long sidx,
+        unsigned long long w, u;
+        parse_key<K64>(cd, nd.k0, nd.k1, w, u);
+        row_fills(st, w, u,
+                  [&](unsigned long long wd, unsigned long long ud, unsigned long long sidx,
                       uint32_t scol, uint32_t depth) {
-                      const unsigned long long ck = cw | p.in_shift;
-                      if (!table_find(p.table, p.cap, ck, u, p.max_probe))
+                      unsigned long long ck0, ck1;
+                      if (!probe_child<K64>(p, cd, wd, ud, ck0, ck1))
                           return false;
                       const unsigned pos = atomicAdd(n_out, 1u);
                       if (pos >= max_out) {
@@ -338,8 +645,8 @@ k_extend_paths(ProbeArgs p, const PathNode *__restrict__ nodes, uint32_t n_nodes
                           return true;
                       }
                       PathNode o;
-                      o.k0 = ck;
-                      o.k1 = u;
+                      o.k0 = ck0;
+                      o.k1 = ck1;
                       o.parent = i;
                       o.nfill = depth;
                       for (uint32_t d = 0; d < (uint32_t)kMaxWidth; d++) {
@@ -353,7 +660,7 @@ k_extend_paths(ProbeArgs p, const PathNode *__restrict__ nodes, uint32_t n_nodes
     }
 }
 
-__global__ void k_select(const ulonglong2 *__restrict__ keys, const unsigned char *__restrict__ alive,
+__global__ void k_select(const ulonglong2 *__restrict__ recs, const unsigned char *__restrict__ alive,
                          unsigned long long n, ulonglong2 *__restrict__ out,
                          unsigned long long *__restrict__ n_out) {
     const unsigned lane = threadIdx.x & 31u;
@@ -368,11 +675,11 @@ __global__ void k_select(const ulonglong2 *__restrict__ keys, const unsigned cha
             b = atomicAdd(n_out, (unsigned long long)__popc(m));
         b = __shfl_sync(0xffffffffu, b, 0);
         if (keep)
-            out[b + __popc(m & ((1u << lane) - 1u))] = keys[i];
+            out[b + __popc(m & ((1u << lane) - 1u))] = recs[i];
     }
 }
 
-__global__ void k_count_pattern(const ulonglong2 *__restrict__ keys, unsigned long long n,
+__global__ void k_count_pattern(const ulonglong2 *__restrict__ recs, unsigned long long n,
                                 unsigned long long mask, unsigned long long value,
                                 unsigned long long *__restrict__ out) {
     const unsigned lane = threadIdx.x & 31u;
@@ -380,7 +687,7 @@ __global__ void k_count_pattern(const ulonglong2 *__restrict__ keys, unsigned lo
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += stride)
-        c += (keys[i].x & mask) == value;
+        c += (recs[i].x & mask) == value;
     for (int o = 16; o > 0; o >>= 1)
         c += __shfl_down_sync(0xffffffffu, c, o);
     if (lane == 0 && c)
@@ -389,57 +696,75 @@ __global__ void k_count_pattern(const ulonglong2 *__restrict__ keys, unsigned lo
 
 }  // namespace
 
-void launch_count_pattern(const ulonglong2 *keys, unsigned long long n, unsigned long long mask,
-                          unsigned long long value, unsigned long long *out, int grid,
-                          cudaStream_t s) {
-    if (n == 0)
-        return;
-    k_count_pattern<<<grid, 256, 0, s>>>(keys, n, mask, value, out);
+cudaError_t expand_max_blocks_per_sm(bool k64, int *n) {
+    return k64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, k_expand<true>, kExpandBlock, 0)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, k_expand<false>, kExpandBlock, 0);
 }
 
-cudaError_t expand_max_blocks_per_sm(int *n) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, k_expand, kExpandBlock, 0);
-}
-
-void launch_expand(const ExpandArgs &a, int grid, cudaStream_t s) {
+void launch_expand(bool k64, const ExpandArgs &a, int grid, cudaStream_t s) {
     if (a.n_chunks == 0)
         return;
-    k_expand<<<grid, kExpandBlock, 0, s>>>(a);
+    if (k64)
+        k_expand<true><<<grid, kExpandBlock, 0, s>>>(a);
+    else
+        k_expand<false><<<grid, kExpandBlock, 0, s>>>(a);
 }
 
-void launch_compact(const CompactArgs &a, int grid, cudaStream_t s) {
+void launch_compact(bool k64, const CompactArgs &a, int grid, cudaStream_t s) {
     if (a.cap == 0)
         return;
-    k_compact<<<grid, kCompactBlock, 0, s>>>(a);
+    if (k64)
+        k_compact<true><<<grid, kCompactBlock, 0, s>>>(a);
+    else
+        k_compact<false><<<grid, kCompactBlock, 0, s>>>(a);
 }
 
-void launch_keyset_insert(const KeySetArgs &t, const ulonglong2 *keys, unsigned long long n,
-                          int grid, cudaStream_t s) {
+void launch_keyset_insert(bool k64, const KeySetArgs &t, const ulonglong2 *recs,
+                          unsigned long long n, int grid, cudaStream_t s) {
     if (n == 0)
         return;
-    k_keyset_insert<<<grid, 256, 0, s>>>(t, keys, n);
+    if (k64)
+        k_keyset_insert<true><<<grid, 256, 0, s>>>(t, recs, n);
+    else
+        k_keyset_insert<false><<<grid, 256, 0, s>>>(t, recs, n);
 }
 
-void launch_mark_alive(const ProbeArgs &p, const ulonglong2 *keys, unsigned long long n,
-                       unsigned char *alive, int grid, cudaStream_t s) {
+void launch_mark_alive(bool k64, const ProbeArgs &p, const ulonglong2 *recs,
+                       unsigned long long n, unsigned char *alive, int grid, cudaStream_t s) {
     if (n == 0)
         return;
-    k_mark_alive<<<grid, kExpandBlock, 0, s>>>(p, keys, n, alive);
+    if (k64)
+        k_mark_alive<true><<<grid, kExpandBlock, 0, s>>>(p, recs, n, alive);
+    else
+        k_mark_alive<false><<<grid, kExpandBlock, 0, s>>>(p, recs, n, alive);
 }
 
-void launch_extend_paths(const ProbeArgs &p, const PathNode *nodes, uint32_t n_nodes,
+void launch_extend_paths(bool k64, const ProbeArgs &p, const PathNode *nodes, uint32_t n_nodes,
                          PathNode *out, unsigned int *n_out, uint32_t max_out,
                          unsigned int *status, int grid, cudaStream_t s) {
     if (n_nodes == 0)
         return;
-    k_extend_paths<<<grid, kExpandBlock, 0, s>>>(p, nodes, n_nodes, out, n_out, max_out, status);
+    if (k64)
+        k_extend_paths<true><<<grid, kExpandBlock, 0, s>>>(p, nodes, n_nodes, out, n_out, max_out,
+                                                           status);
+    else
+        k_extend_paths<false><<<grid, kExpandBlock, 0, s>>>(p, nodes, n_nodes, out, n_out,
+                                                            max_out, status);
 }
 
-void launch_select(const ulonglong2 *keys, const unsigned char *alive, unsigned long long n,
+void launch_select(const ulonglong2 *recs, const unsigned char *alive, unsigned long long n,
                    ulonglong2 *out, unsigned long long *n_out, int grid, cudaStream_t s) {
     if (n == 0)
         return;
-    k_select<<<grid, 256, 0, s>>>(keys, alive, n, out, n_out);
+    k_select<<<grid, 256, 0, s>>>(recs, alive, n, out, n_out);
+}
+
+void launch_count_pattern(const ulonglong2 *recs, unsigned long long n, unsigned long long mask,
+                          unsigned long long value, unsigned long long *out, int grid,
+                          cudaStream_t s) {
+    if (n == 0)
+        return;
+    k_count_pattern<<<grid, 256, 0, s>>>(recs, n, mask, value, out);
 }
 
 }  // namespace d4e

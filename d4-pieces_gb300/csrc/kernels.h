@@ -1,4 +1,8 @@
 // kernels.h -- launch wrappers for the sm_103a kernels of the tiling engine.
+//
+// Frontier records are passed as ulonglong2 arrays in both key encodings:
+// K64 records are {key, count}; K128 records are {window, tag} keys with the
+// counts in a separate u64 array.
 #pragma once
 
 #include <cstdint>
@@ -12,80 +16,86 @@ struct ExpandArgs {
     const Seg *segs;
     uint32_t n_segs;
     uint64_t n_chunks;
-    uint64_t chunk_states;
+    uint64_t chunk_states;           // work items per chunk
+    uint32_t fan;                    // >0: split each state's walk by its first placement
+                                     // (work item = state * fan + first choice)
     const InstDesc *insts;
     const Plc *plc;
-    const ulonglong2 *keys;
-    const unsigned long long *cnts;
-    Slot *table;
-    unsigned long long cap;         // table slots (any value >= 1)
-    unsigned int *inst_unique;      // per instance: new keys claimed
-    unsigned long long *n_raw;      // children produced (all instances)
+    const ulonglong2 *recs;          // frontier (K64 records / K128 keys)
+    const unsigned long long *cnts;  // K128 counts
+    void *table;                     // Slot16[cap] (K64) or Slot32[cap] (K128)
+    unsigned long long cap;          // table slots (any value >= 1)
+    unsigned int *inst_unique;       // per instance: new keys claimed
+    unsigned long long *n_raw;       // children produced (all instances)
     unsigned int *status;
-    unsigned long long *work;       // dynamic chunk counter, zeroed before launch
+    unsigned long long *work;        // dynamic chunk counter, zeroed before launch
     unsigned int max_probe;
 };
 
 struct CompactArgs {
-    Slot *table;
+    void *table;
     unsigned long long cap;
-    unsigned long long *cursor;     // per instance: next output position, or kCursorFinal
-    ulonglong2 *out_keys;
-    unsigned long long *out_cnts;
-    unsigned long long *results;    // per instance: summed counts of final states
-    unsigned int *final_states;     // per instance: number of final states
+    unsigned long long *cursor;      // per instance: next output position, or kCursorFinal
+    ulonglong2 *out_recs;
+    unsigned long long *out_cnts;    // K128 counts
+    unsigned long long *results;     // per instance: summed counts of final states
+    unsigned int *final_states;      // per instance: number of final states
+    uint32_t inst_off;               // K64: position of the instance id in a key
+    unsigned long long inst_mask;    // K64: instance id mask (after shifting)
 };
 
 // Resident k_expand blocks per SM (for sizing its persistent grid).
-cudaError_t expand_max_blocks_per_sm(int *n);
+cudaError_t expand_max_blocks_per_sm(bool k64, int *n);
 
 // Expand every state of every chunk by every whole-row fill and insert the
 // children into the open-addressing table (counts summed).
-void launch_expand(const ExpandArgs &a, int grid, cudaStream_t s);
+void launch_expand(bool k64, const ExpandArgs &a, int grid, cudaStream_t s);
 
 // Move the table's occupied slots into per-instance frontier segments (or into
 // the per-instance results for instances finishing their last row) and clear
 // the table.
-void launch_compact(const CompactArgs &a, int grid, cudaStream_t s);
+void launch_compact(bool k64, const CompactArgs &a, int grid, cudaStream_t s);
 
 // Solution reconstruction -------------------------------------------------
 struct KeySetArgs {
-    Slot *table;
+    void *table;
     unsigned long long cap;
     unsigned int *status;
     unsigned int max_probe;
 };
 
-// Insert n keys into the (cleared) table as a membership set.
-void launch_keyset_insert(const KeySetArgs &t, const ulonglong2 *keys, unsigned long long n,
-                          int grid, cudaStream_t s);
+// Insert the keys of n records into the (cleared) table as a membership set.
+void launch_keyset_insert(bool k64, const KeySetArgs &t, const ulonglong2 *recs,
+                          unsigned long long n, int grid, cudaStream_t s);
 
 struct ProbeArgs {
     const InstDesc *insts;
     const Plc *plc;
     uint32_t inst;                  // single instance per launch
     uint32_t row;                   // row being completed
-    unsigned long long in_shift;
-    const Slot *table;              // membership set of the next level's live states
+    unsigned long long in_shift;    // K128
+    unsigned long long hi_board;    // K64
+    unsigned long long tag;
+    const void *table;              // membership set of the next level's live states
     unsigned long long cap;
     unsigned int max_probe;
 };
 
 // alive[i] = 1 when state i has at least one child in the set.
-void launch_mark_alive(const ProbeArgs &p, const ulonglong2 *keys, unsigned long long n,
-                       unsigned char *alive, int grid, cudaStream_t s);
+void launch_mark_alive(bool k64, const ProbeArgs &p, const ulonglong2 *recs,
+                       unsigned long long n, unsigned char *alive, int grid, cudaStream_t s);
 
 // For every node, emit one PathNode per (row fill, child in the set).
-void launch_extend_paths(const ProbeArgs &p, const PathNode *nodes, uint32_t n_nodes,
+void launch_extend_paths(bool k64, const ProbeArgs &p, const PathNode *nodes, uint32_t n_nodes,
                          PathNode *out, unsigned int *n_out, uint32_t max_out,
                          unsigned int *status, int grid, cudaStream_t s);
 
-// Keep keys whose alive flag is set (order preserved).
-void launch_select(const ulonglong2 *keys, const unsigned char *alive, unsigned long long n,
+// Keep records whose alive flag is set (order not preserved).
+void launch_select(const ulonglong2 *recs, const unsigned char *alive, unsigned long long n,
                    ulonglong2 *out, unsigned long long *n_out, int grid, cudaStream_t s);
 
-// *out += number of keys with (key.x & mask) == value.
-void launch_count_pattern(const ulonglong2 *keys, unsigned long long n, unsigned long long mask,
+// *out += number of records with (rec.x & mask) == value.
+void launch_count_pattern(const ulonglong2 *recs, unsigned long long n, unsigned long long mask,
                           unsigned long long value, unsigned long long *out, int grid,
                           cudaStream_t s);
 

@@ -19,6 +19,8 @@ CSRC = PKG_ROOT / "csrc"
 OBJ_DIR = PKG_ROOT / "_build"
 LIB_DIR = PKG_ROOT / "lib"
 LIB_PATH = LIB_DIR / "libd4e.so"
+HOST_DIR = PKG_ROOT / "host"
+EXAMPLE_PATH = LIB_DIR / "example_step"
 INCLUDE = PKG_ROOT.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -86,7 +88,25 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
+    _build_example(verbose)
     return LIB_PATH
+
+
+def _build_example(verbose: bool) -> Path:
+    """The C++ facade's example driver, linked against libd4e.so."""
+    src = HOST_DIR / "example_step.cpp"
+    deps = [src, HOST_DIR / "searcher_cuda.h", INCLUDE / "d4e.h", LIB_PATH]
+    if not _needs_rebuild(EXAMPLE_PATH, deps):
+        return EXAMPLE_PATH
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-Wall", "-I", str(HOST_DIR),
+           str(src), "-o", str(EXAMPLE_PATH), "-L", str(LIB_DIR), "-ld4e",
+           "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"example build failed\n{r.stdout}\n{r.stderr}")
+    return EXAMPLE_PATH
 
 
 if __name__ == "__main__":

@@ -54,6 +54,8 @@ class Stats(C.Structure):
         ("expand_ms", C.c_double),
         ("compact_ms", C.c_double),
         ("run_ms", C.c_double),
+        ("record_bytes", C.c_uint64),
+        ("slot_bytes", C.c_uint64),
     ]
 
     def as_dict(self) -> dict:

@@ -175,6 +175,16 @@ def single_large(seed: int) -> Problem:
                    meta={"seed": seed, "holes": sorted(holes)})
 
 
+def medium_board(seed: int = 77) -> Problem:
+    """8 x 10 board minus 2 cells (78 cells) with 4..6-cell pieces of exactly
+    that area (the profiling-size relative of single_large)."""
+    rng = random.Random(seed)
+    rows = [0xFF] * 6 + [0xF7, 0xEF] + [0xFF] * 2
+    sizes = _piece_sizes(rng, 78, 4, 6)
+    types, counts = merge_pieces([grow_polyomino(rng, k) for k in sizes])
+    return Problem(8, 10, rows, types, counts, FULL_D4, name=f"medium 8x10 seed {seed}")
+
+
 def batched_instance(rng: random.Random, idx: int = 0) -> Problem:
     W = rng.randint(5, 8)
     H = rng.randint(5, 12)

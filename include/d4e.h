@@ -39,9 +39,9 @@ extern "C" {
 #define D4E_ERR_UNSUPPORTED (-4) /* outside the engine's limits (see below) */
 #define D4E_ERR_STATE (-5)       /* call not valid in the handle's current state */
 
-/* Limits: board width 1..8, height 1..64, <= 40 piece copies per puzzle,
- * <= 255 placements anchored at one column, pieces no taller than 64/width
- * rows. */
+/* Limits: board width 1..8, height 1..64, <= 40 piece types whose copy
+ * counters (bit_length(count) bits each) fit in 40 bits, <= 255 placements
+ * anchored at one column, pieces no taller than 64/width rows. */
 
 /* Message of the last failing call on this thread ("" if none). */
 const char *d4e_last_error(void);
@@ -163,6 +163,8 @@ typedef struct d4e_stats {
     double expand_ms;           /* device time of k_expand (CUDA events) */
     double compact_ms;          /* device time of k_compact (CUDA events) */
     double run_ms;              /* CUDA-event time from the first row's start to the last row's end */
+    uint64_t record_bytes;      /* bytes per frontier state: 16 (packed 64-bit keys) or 24 */
+    uint64_t slot_bytes;        /* bytes per hash-table slot: 16 or 32 */
 } d4e_stats;
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st);

@@ -406,6 +406,8 @@ typedef struct {
     dp_vec *shards; /* T shard buffers for this worker */
     int T;
     uint64_t cnt;
+    uint64_t pushed, limit; /* children produced by this worker, cap (0 = none) */
+    volatile int *abort;
 } dp_expand_ctx;
 
 static void dp_fill(dp_expand_ctx *e, u128 open, uint64_t used)
@@ -413,9 +415,13 @@ static void dp_fill(dp_expand_ctx *e, u128 open, uint64_t used)
     const dp_tab *t = e->tab;
     int W = t->W;
     u128 rowm = (((u128)1 << W) - 1) << (e->row * W);
+    if (*e->abort)
+        return;
     if (!(open & rowm)) {
         dp_state s = { open, used, e->cnt };
         vec_push(&e->shards[dp_hash(&s) % (uint64_t)e->T], &s);
+        if (e->limit && ++e->pushed > e->limit)
+            *e->abort = 1;
         return;
     }
     int pos = ctz128(open);
@@ -442,7 +448,13 @@ typedef struct {
     size_t lo, hi;
     dp_vec **shards; /* [worker][shard] */
     dp_vec *out;     /* per shard output */
+    uint64_t limit;  /* children per worker (0 = none) */
+    volatile int *abort;
+    double deadline; /* absolute time limit (0 = none) */
+    size_t expanded; /* input states fully expanded */
 } dp_job;
+
+static double now_s(void);
 
 static void *dp_expand_worker(void *arg)
 {
@@ -452,9 +464,19 @@ static void *dp_expand_worker(void *arg)
     e.row = j->row;
     e.T = j->T;
     e.shards = j->shards[j->id];
-    for (size_t i = j->lo; i < j->hi; i++) {
+    e.pushed = 0;
+    e.limit = j->limit;
+    e.abort = j->abort;
+    j->expanded = 0;
+    for (size_t i = j->lo; i < j->hi && !*j->abort; i++) {
+        if (j->deadline > 0 && ((i - j->lo) & 255) == 0 && now_s() > j->deadline) {
+            *j->abort = 1;
+            break;
+        }
         e.cnt = j->in[i].cnt;
         dp_fill(&e, j->in[i].open, j->in[i].used);
+        if (!*j->abort)
+            j->expanded++;
     }
     return NULL;
 }
@@ -508,7 +530,7 @@ static double now_s(void)
 }
 
 int32_t or_rowdp(const or_problem *p, int32_t threads, double max_seconds,
-                 uint64_t *level_sizes, uint64_t *count,
+                 uint64_t max_children, uint64_t *level_sizes, uint64_t *count,
                  int32_t *levels_done, uint64_t *states_total)
 {
     or_ctx c;
@@ -565,6 +587,7 @@ int32_t or_rowdp(const or_problem *p, int32_t threads, double max_seconds,
     double t0 = now_s();
     uint64_t tot = 0;
     int done = 0;
+    volatile int abort_flag = 0;
     for (int r = 0; r < c.H; r++) {
         for (int w = 0; w < T; w++) {
             jobs[w].tab = &tab;
@@ -576,7 +599,11 @@ int32_t or_rowdp(const or_problem *p, int32_t threads, double max_seconds,
             jobs[w].hi = cur.n * (size_t)(w + 1) / (size_t)T;
             jobs[w].shards = shards;
             jobs[w].out = outs;
+            jobs[w].limit = max_children ? (max_children + (uint64_t)T - 1) / (uint64_t)T : 0;
+            jobs[w].abort = &abort_flag;
+            jobs[w].deadline = max_seconds > 0 ? t0 + max_seconds : 0;
         }
+        const size_t jobs_in = cur.n;
         if (T == 1)
             dp_expand_worker(&jobs[0]);
         else {
@@ -584,6 +611,15 @@ int32_t or_rowdp(const or_problem *p, int32_t threads, double max_seconds,
                 pthread_create(&th[w], NULL, dp_expand_worker, &jobs[w]);
             for (int w = 0; w < T; w++)
                 pthread_join(th[w], NULL);
+        }
+        if (abort_flag) {
+            /* partial level: count the states expanded, drop their children */
+            for (int w = 0; w < T; w++) {
+                tot += jobs[w].expanded;
+                for (int s = 0; s < T; s++)
+                    shards[w][s].n = 0;
+            }
+            break;
         }
         if (T == 1)
             dp_merge_worker(&jobs[0]);
@@ -599,7 +635,7 @@ int32_t or_rowdp(const or_problem *p, int32_t threads, double max_seconds,
                 vec_push(&cur, &outs[w].v[i]);
         if (level_sizes)
             level_sizes[r] = cur.n;
-        tot += cur.n;
+        tot += jobs_in;
         done = r + 1;
         if (max_seconds > 0 && now_s() - t0 > max_seconds)
             break;

@@ -66,12 +66,15 @@ void or_canonical_grid(const or_problem *p, const int8_t *grid, int8_t *out);
 
 /* Exact row-by-row frontier DP.  level_sizes[r] = number of distinct states
  * after completing row r (r = 0..H-1).  *count = number of tilings (mod
- * 2^64).  threads >= 1.  max_seconds > 0 stops after the first level whose
- * completion pushes the elapsed time past the budget; *levels_done reports
- * how many rows were completed and *states_total the summed frontier sizes.
+ * 2^64).  threads >= 1.  max_seconds > 0 stops once the elapsed time passes
+ * the budget and max_children > 0 once a level's children exceed it (host
+ * memory bound), both in the middle of a level if need be.  *levels_done
+ * reports how many rows were completed and *states_total how many frontier
+ * states were expanded (whole rows plus the expanded part of an interrupted
+ * row).
  * Returns 0 on success, -1 on bad input. */
 int32_t or_rowdp(const or_problem *p, int32_t threads, double max_seconds,
-                 uint64_t *level_sizes, uint64_t *count,
+                 uint64_t max_children, uint64_t *level_sizes, uint64_t *count,
                  int32_t *levels_done, uint64_t *states_total);
 
 /* Independent cover check of one tiling given as placements:

@@ -55,7 +55,7 @@ def _load():
         lib.or_canonical_grid.argtypes = [C.POINTER(_Problem), C.POINTER(C.c_int8),
                                           C.POINTER(C.c_int8)]
         lib.or_rowdp.restype = C.c_int32
-        lib.or_rowdp.argtypes = [C.POINTER(_Problem), C.c_int32, C.c_double,
+        lib.or_rowdp.argtypes = [C.POINTER(_Problem), C.c_int32, C.c_double, C.c_uint64,
                                  C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_uint64)]
         lib.or_check_tiling.restype = C.c_int32
@@ -111,14 +111,16 @@ def canonical_set(p, grids) -> set:
     return {canonical_grid(p, g).tobytes() for g in grids}
 
 
-def rowdp(p, threads: int = 1, max_seconds: float = 0.0) -> dict:
+def rowdp(p, threads: int = 1, max_seconds: float = 0.0, max_children: int = 0) -> dict:
+    """Exact row DP; max_seconds / max_children bound a sample (see
+    d4oracle.h)."""
     st, keep = _prob(p)
     sizes = (C.c_uint64 * max(p.height, 1))()
     count = C.c_uint64()
     done = C.c_int32()
     total = C.c_uint64()
-    r = _load().or_rowdp(C.byref(st), threads, max_seconds, sizes, C.byref(count),
-                         C.byref(done), C.byref(total))
+    r = _load().or_rowdp(C.byref(st), threads, max_seconds, max_children, sizes,
+                         C.byref(count), C.byref(done), C.byref(total))
     if r != 0:
         raise ValueError("oracle rejected the problem")
     return {"level_sizes": list(sizes)[: done.value], "count": int(count.value),

@@ -137,31 +137,43 @@ def test_batch_equals_alone(E):
 
 
 def test_batched_mix_matches_oracle(E, oracle):
+    """Batched-mix instances small enough for the CPU row DP (<= 36 cells)
+    against the oracle, counted in one mixed batch."""
     from d4gb.problem import batched_mix
 
-    probs = batched_mix(5, 24)
+    probs = [p for p in batched_mix(5, 400) if p.cells <= 36][:24]
+    assert len(probs) >= 8
     got, _ = E.batch_count(probs)
     for p, g in zip(probs, got):
         assert g == oracle.rowdp(p, threads=4)["count"], p.name
 
 
+def test_batched_mix_flip_invariance(E):
+    """Batched-mix instances beyond the CPU oracle's reach (37..48 cells):
+    each count equals its mirrored board's count (all 8 transforms allowed),
+    in one batch of 2 x 32 puzzles."""
+    from d4gb.problem import Problem, batched_mix
+
+    probs = [p for p in batched_mix(9, 600) if 37 <= p.cells <= 48][:32]
+    flipped = [Problem(p.width, p.height, p.rows[::-1], p.shapes, p.counts, p.sym) for p in probs]
+    got, _ = E.batch_count(probs + flipped)
+    assert got[:32] == got[32:]
+
+
 def test_d4_invariance_on_tall_board(E):
     """Size-independent property: a board and its mirror images have the same
-    number of tilings when all 8 transforms are allowed."""
-    from d4gb.problem import single_large
+    number of tilings when all 8 transforms are allowed (8 x 10 board, 16
+    random 4..6-cell pieces of exactly the board's area)."""
+    from d4gb.problem import Problem, medium_board
 
-    p = single_large(2)
-    p.rows = [0xFF] * 6 + [0xF7, 0xEF] + [0xFF] * 2     # 8x10, 78 cells
-    p.height = 10
-    area = sum(bin(r).count("1") for r in p.rows)
-    # keep pieces summing to at most the area (sub-multisets may tile)
+    p = medium_board(77)
+    rows, types, counts = p.rows, p.shapes, p.counts
     n = gpu_count(E, p)[1]
-    flip_y = type(p)(p.width, p.height, p.rows[::-1], p.shapes, p.counts, p.sym)
-    flip_x = type(p)(p.width, p.height,
-                     [int(f"{r:08b}"[::-1], 2) for r in p.rows], p.shapes, p.counts, p.sym)
+    flip_y = Problem(8, 10, rows[::-1], types, counts, 0xFF)
+    flip_x = Problem(8, 10, [int(f"{r:08b}"[::-1], 2) for r in rows], types, counts, 0xFF)
     assert gpu_count(E, flip_y)[1] == n
     assert gpu_count(E, flip_x)[1] == n
-    assert area == 78
+    assert n == 4952290238   # computed once by the oracle's row DP (237 s on 8 threads)
 
 
 def test_width_one_to_eight(E, oracle):
@@ -173,13 +185,28 @@ def test_width_one_to_eight(E, oracle):
         assert gpu_count(E, p)[1] == want, w
 
 
-def test_forty_copies_and_limits(E, oracle):
+def test_many_copies_and_limits(E, oracle):
     from d4gb.problem import Problem
 
     p = Problem(8, 5, [0xFF] * 5, [3], [20], 0xFF)     # dominoes, 20 copies
     assert gpu_count(E, p)[1] == oracle.rowdp(p)["count"]
     p = Problem(8, 5, [0xFF] * 5, [1, 3], [20, 20], 0xFF)  # 40 copies
     assert gpu_count(E, p)[1] == oracle.rowdp(p)["count"]
+    p = Problem(8, 8, [0xFF] * 8, [1, 3], [40, 12], 0xFF)  # 52 copies (6 + 4 counter bits)
+    assert gpu_count(E, p)[1] == oracle.rowdp(p)["count"]
     with pytest.raises(E.D4Error) as e:
-        E.Frow([1], [41], 0xFF, 8, device=0)
+        E.Frow([1, 3] * 11, [3] * 22, 0xFF, 8, device=0)
     assert e.value.code == -4
+
+
+def test_cpp_facade_reference_loop(E):
+    """The reference's caller loop (Searcher::step) through the C++ facade."""
+    import subprocess
+
+    from d4gb import build
+
+    r = subprocess.run([str(build.EXAMPLE_PATH), "0xFFFFFFE7E7FFFFFF", "5", "5"],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip().splitlines()[-1] == "count 520"
+    assert r.stdout.count("height=") == 8

@@ -101,8 +101,9 @@ def test_frow_rejects_bad_input(engine):
     with pytest.raises(engine.D4Error) as e:
         engine.Frow([1 | 4], [1], 0xFF, 8, device=None)   # disconnected
     assert e.value.code == -1
+    engine.Frow([1], [41], 0xFF, 8, device=None)          # 41 copies: a 6-bit counter
     with pytest.raises(engine.D4Error) as e:
-        engine.Frow([1], [41], 0xFF, 8, device=None)      # > 40 copies
+        engine.Frow([1, 3] * 11, [3] * 22, 0xFF, 8, device=None)   # 22 x 2 bits > 40
     assert e.value.code == -4
     # an 8-cell bar fits a 4-wide board upright only (8 rows <= 64 / 4): accepted
     f = engine.Frow([255], [1], 0xFF, 4, device=None)
@@ -153,3 +154,14 @@ def test_empty_area_board_layout():
     ea = p.empty_area()
     assert ea == 0xFFFFFFE7E7FFFFFF
     assert bin(ea).count("1") == 60
+
+
+def test_cpp_facade_builds_and_fails_like_reference_without_gpu(engine):
+    from d4gb import build
+
+    exe = build.EXAMPLE_PATH
+    assert exe.exists()
+    if engine.device_count() > 0:
+        pytest.skip("a GPU is present")
+    r = subprocess.run([str(exe), "0xFFFFFFE7E7FFFFFF", "5", "5"], capture_output=True, text=True)
+    assert r.returncode == 1 and "no CUDA device" in r.stderr
