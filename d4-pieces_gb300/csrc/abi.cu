@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/d4e.h"
+#include "abi_util.h"
 #include "engine.h"
 #include "kernels.h"
 
@@ -36,6 +37,14 @@ int guarded(F &&f) {
 }
 
 }  // namespace
+
+namespace d4e {
+
+int abi_fail(int code, const std::string &msg) { return fail(code, msg); }
+
+void abi_clear_error() { g_err.clear(); }
+
+}  // namespace d4e
 
 struct d4e_frow {
     std::vector<uint64_t> shapes;

@@ -109,6 +109,7 @@ _sig("d4e_searcher_destroy", None, C.c_void_p)
 _sig("d4e_batch_count", C.c_int, C.POINTER(Instance), C.c_uint32, C.c_uint32, C.c_int32, _u64p,
      C.POINTER(Stats))
 _sig("d4e_canonical_grid", C.c_int, C.c_uint32, C.c_uint32, _u8p, _i8p, _i8p)
+_sig("d4e_count_noalloc", C.c_int, C.POINTER(Instance), C.c_void_p, _u64p, _u64p)
 
 
 def lib() -> C.CDLL:
@@ -295,6 +296,16 @@ def count(problem, device: int = 0) -> int:
     s = CudaSearcher(f, rows=problem.rows)
     s.run()
     return s.count()
+
+
+def count_noalloc(problem, stream=None):
+    """(tilings, summed frontier sizes) through d4e_count_noalloc, the entry
+    point that allocates no device memory (current device)."""
+    arr, keep = _instances([problem])
+    cnt = C.c_uint64()
+    states = C.c_uint64()
+    _check(_lib.d4e_count_noalloc(arr, stream, C.byref(cnt), C.byref(states)))
+    return cnt.value, states.value
 
 
 def canonical_grid(problem, grid) -> np.ndarray:

@@ -201,6 +201,35 @@ typedef struct d4e_instance {
 int d4e_batch_count(const d4e_instance *insts, uint32_t n, uint32_t flags, int32_t device,
                     uint64_t *counts, d4e_stats *st);
 
+/* ------------------------------------------------------------------------
+ * Counting without device allocation.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc: processes that reserve their
+ * device memory once at start-up and may not grow it afterwards (a server
+ * sharing the GPU with other tenants under a fixed budget, where an
+ * allocation in the middle of a request can fail or stall behind other
+ * work), and code running under a caller-owned memory pool that forbids the
+ * runtime allocator.  d4e_count_noalloc allocates no device memory and calls
+ * no allocating library routine: every buffer it needs (descriptor,
+ * placement table, two frontier buffers, the de-duplication table, counters)
+ * lives in one file-scope __device__ array of D4E_NOALLOC_SCRATCH_BYTES that
+ * every GPU loading the library holds until the process exits.
+ *
+ * Works on the current CUDA device; stream may be NULL (legacy default
+ * stream).  The first call on each device resolves the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  All calls share the array and it keeps the last call's
+ * contents (each call clears what it needs): calls that overlap on the GPU
+ * -- from several host threads or on several streams of one device -- race
+ * and must be serialised by the caller.  A puzzle whose row frontier exceeds
+ * the array's capacity (about 1.0M states with packed 64-bit keys, 0.59M
+ * otherwise) fails with D4E_ERR_UNSUPPORTED.  *count receives the number of
+ * tilings; states (may be NULL) the sum of the per-row frontier sizes. */
+#define D4E_NOALLOC_SCRATCH_BYTES (64u << 20)
+
+int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_t *count,
+                      uint64_t *states);
+
 /* Canonical D4 form of a solution type grid over the board's own symmetry
  * (lexicographic minimum over the transforms mapping the board onto
  * itself). */
