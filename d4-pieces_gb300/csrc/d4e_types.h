@@ -66,6 +66,16 @@ struct InstDesc {
     uint32_t used_bits;
     uint16_t col_off[kMaxWidth];   // placements anchored at column c: [col_off, col_off + col_len)
     uint16_t col_len[kMaxWidth];
+    // Candidate filters (bitsets over a column's placements, `fwords` u64
+    // words each, in the global filter array from filt_off on):
+    //   row-0 filter of column c, pattern p = current row >> (c + 1):
+    //     placements whose row-0 cells fit  -> filt_off + f0_off[c] + p * fwords
+    //   row-1 filter of column c, pattern q = next row:
+    //     placements whose row-1 cells fit  -> filt_off + f1_off[c] + q * fwords
+    uint32_t filt_off;
+    uint32_t fwords;
+    uint32_t f0_off[kMaxWidth];
+    uint32_t f1_off[kMaxWidth];
     TypeField types[kMaxTypes];
     uint8_t rows[kMaxHeight];      // board rows, bit c = cell to cover
 };

@@ -109,6 +109,7 @@ Engine::~Engine() {
         if (e)
             cudaEventDestroy(e);
     plc_.release();
+    filt_.release();
     insts_.release();
     inst_unique_.release();
     cursor_.release();
@@ -171,6 +172,13 @@ uint32_t Engine::add(const InstanceSpec &sp) {
     d.win_rows = 64 / sp.width;
     d.n_plc = (uint32_t)in.lib.plc.size();
     d.plc_off = (uint32_t)plc_total_;
+    d.filt_off = (uint32_t)filt_total_;
+    d.fwords = in.lib.fwords;
+    for (int c = 0; c < kMaxWidth; c++) {
+        d.f0_off[c] = in.lib.f0_off[c];
+        d.f1_off[c] = in.lib.f1_off[c];
+    }
+    filt_total_ += in.lib.filters.size();
     d.n_types = (uint32_t)in.lib.fields.size();
     d.dyn_bits = in.lib.dyn_bits;
     d.used_bits = in.lib.used_bits;
@@ -245,6 +253,20 @@ void Engine::flush_uploads() {
                    "upload placements");
     tot_.h2d_bytes += plc.size() * sizeof(Plc);
     plc_uploaded_ = plc_total_;
+    std::vector<unsigned long long> filt;
+    filt.reserve(filt_total_ - filt_uploaded_);
+    for (uint32_t id = lo; id < hi; id++) {
+        const auto &v = inst_[id].lib.filters;
+        filt.insert(filt.end(), v.begin(), v.end());
+    }
+    filt_.reserve(std::max<uint64_t>(filt_total_, 1), stream_, filt_uploaded_);
+    if (!filt.empty())
+        cuda_check(cudaMemcpyAsync(filt_.p + filt_uploaded_, filt.data(),
+                                   filt.size() * sizeof(unsigned long long),
+                                   cudaMemcpyHostToDevice, stream_),
+                   "upload filters");
+    tot_.h2d_bytes += filt.size() * sizeof(unsigned long long);
+    filt_uploaded_ = filt_total_;
     cuda_check(cudaMemsetAsync(results_.p + lo, 0, (hi - lo) * sizeof(unsigned long long), stream_),
                "memset");
     cuda_check(cudaMemsetAsync(final_states_.p + lo, 0, (hi - lo) * sizeof(unsigned int), stream_),
@@ -388,22 +410,27 @@ StepStats Engine::step() {
     // Segments of the active instances, in frontier order.
     std::sort(active_.begin(), active_.end(),
               [&](uint32_t a, uint32_t b) { return inst_[a].seg_begin < inst_[b].seg_begin; });
-    // Small frontiers (fewer states than a quarter of the resident lanes) are
-    // split: each state's walk is cut by its first placement into `fan` work
-    // items, so a handful of states still spreads over the whole GPU.
+    // A state's walk can be cut by its first placement into `fan` work items
+    // (fan = the longest placement list of a column), so a handful of states
+    // still fills the GPU.
     int occ = expand_occupancy();
     const uint64_t slots = (uint64_t)sms_ * (uint64_t)occ;
+    // Only frontiers with fewer states than a quarter of the resident lanes
+    // are split; larger ones already fill the GPU, and warps fetch chunks
+    // independently, so a heavy state delays only its own lane.
     uint32_t fan = 0;
-    if (n_cur_ * 4 < slots * 256) {
+    if (n_cur_ * 4 < slots * 256)
         for (uint32_t id : active_)
             for (int c = 0; c < kMaxWidth; c++)
                 fan = std::max<uint32_t>(fan, inst_[id].desc.col_len[c]);
-        fan = std::max<uint32_t>(fan, 1);
-    }
+    if (fan <= 1)
+        fan = 0;
     const uint64_t items = n_cur_ * (fan ? fan : 1);
-    // Chunk size: about four chunks per resident CTA, within [64, chunk_states].
-    uint64_t chunk = (items + 4 * slots - 1) / (4 * slots);
-    chunk = std::min<uint64_t>(std::max<uint64_t>(round_up(chunk, 64), 64), opts_.chunk_states);
+    // Warps take chunks independently: about eight chunks per resident warp,
+    // within [32, chunk_states] items.
+    const uint64_t warps = slots * 8;
+    uint64_t chunk = (items + 8 * warps - 1) / (8 * warps);
+    chunk = std::min<uint64_t>(std::max<uint64_t>(round_up(chunk, 32), 32), opts_.chunk_states);
     std::vector<Seg> segs;
     segs.reserve(active_.size());
     uint64_t n_chunks = 0;
@@ -456,6 +483,7 @@ StepStats Engine::step() {
         a.fan = fan;
         a.insts = insts_.p;
         a.plc = plc_.p;
+        a.filt = filt_.p;
         a.recs = keys_[cur_].p;
         a.cnts = cnts_[cur_].p;
         a.table = table_.p;

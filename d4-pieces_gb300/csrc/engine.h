@@ -64,7 +64,7 @@ struct EngineOpts {
     uint32_t max_probe = 512;
     bool keep_levels = false;      // retain every level (needed for solutions; one instance)
     double target_load = 0.5;      // hash table load factor aimed at when sizing
-    uint64_t chunk_states = 4096;  // largest number of frontier states per CTA work item
+    uint64_t chunk_states = 1024;  // largest number of work items a warp takes at once
     uint64_t max_frontier = 0;     // abort when a row yields more states (0 = no limit)
     KeyMode key_mode = KeyMode::Auto;  // Auto: K64 when every instance's packed key fits
 };
@@ -182,6 +182,8 @@ private:
 
     DevBuf<Plc> plc_;
     uint64_t plc_total_ = 0, plc_uploaded_ = 0;
+    DevBuf<unsigned long long> filt_;
+    uint64_t filt_total_ = 0, filt_uploaded_ = 0;
     DevBuf<InstDesc> insts_;
     DevBuf<unsigned int> inst_unique_;
     DevBuf<unsigned long long> cursor_;

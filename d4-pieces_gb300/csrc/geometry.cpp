@@ -237,6 +237,38 @@ std::string build_piece_lib(const uint64_t *shapes, const uint32_t *counts, uint
             return "more than 255 placements anchored at one column";
         out.col_len[col] = (uint16_t)len;
     }
+
+    // Candidate filters: for column c, bitsets over its placements of those
+    // whose row-0 cells fit a row-0 pattern (indexed by the bits right of c;
+    // c itself is always empty at that point) and of those whose row-1 cells
+    // fit a row-1 pattern.
+    uint32_t maxlen = 1;
+    for (uint32_t col = 0; col < width; col++)
+        maxlen = std::max<uint32_t>(maxlen, out.col_len[col]);
+    out.fwords = (maxlen + 63) / 64;
+    const uint32_t FW = out.fwords;
+    const uint64_t rowmask = (1ull << width) - 1ull;
+    for (uint32_t col = 0; col < width; col++) {
+        const uint32_t n0 = 1u << (width - 1 - col);
+        out.f0_off[col] = (uint32_t)out.filters.size();
+        out.filters.resize(out.filters.size() + (size_t)n0 * FW, 0ull);
+        for (uint32_t p = 0; p < n0; p++) {
+            const uint64_t row0 = ((uint64_t)p << (col + 1)) | (1ull << col);
+            for (uint32_t i = 0; i < out.col_len[col]; i++) {
+                const uint64_t m0 = out.plc[out.col_off[col] + i].mask & rowmask;
+                if (!(m0 & ~row0))
+                    out.filters[out.f0_off[col] + (size_t)p * FW + i / 64] |= 1ull << (i % 64);
+            }
+        }
+        out.f1_off[col] = (uint32_t)out.filters.size();
+        out.filters.resize(out.filters.size() + ((size_t)1 << width) * FW, 0ull);
+        for (uint32_t q = 0; q < (1u << width); q++)
+            for (uint32_t i = 0; i < out.col_len[col]; i++) {
+                const uint64_t m1 = (out.plc[out.col_off[col] + i].mask >> width) & rowmask;
+                if (!(m1 & ~(uint64_t)q))
+                    out.filters[out.f1_off[col] + (size_t)q * FW + i / 64] |= 1ull << (i % 64);
+            }
+    }
     return {};
 }
 

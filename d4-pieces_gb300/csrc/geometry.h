@@ -45,6 +45,11 @@ struct PieceLib {
     std::vector<uint32_t> plc_orient;    // transform index per placement
     uint16_t col_off[kMaxWidth] = {};
     uint16_t col_len[kMaxWidth] = {};
+    // Candidate filters (see InstDesc): bitsets of `fwords` u64 words.
+    uint32_t fwords = 1;
+    uint32_t f0_off[kMaxWidth] = {};
+    uint32_t f1_off[kMaxWidth] = {};
+    std::vector<uint64_t> filters;
 };
 
 // Builds the tables; returns an empty string on success, else the reason.

@@ -277,55 +277,84 @@ struct WarpStage {
     unsigned long long k0[kStage];
     unsigned long long k1[kStage];
     unsigned long long cnt[kStage];
+    uint32_t inst[kStage];
 };
 
 template <bool K64>
 __device__ __forceinline__ void flush_children(const ExpandArgs &a, const WarpStage &ws, int base,
-                                               int n, uint32_t inst, unsigned lane) {
+                                               int n, unsigned lane) {
     // Lane i inserts child base + i: up to 32 independent inserts in flight.
     int r = 2;
+    uint32_t inst = 0xFFFFFFFFu;
     if ((int)lane < n) {
         const int j = base + (int)lane;
+        inst = ws.inst[j];
         if constexpr (K64)
             r = insert64(static_cast<Slot16 *>(a.table), a.cap, ws.k0[j], ws.cnt[j], a.max_probe);
         else
             r = insert128(static_cast<Slot32 *>(a.table), a.cap, ws.k0[j], ws.k1[j], ws.cnt[j],
                           a.max_probe);
     }
-    const unsigned fresh = __ballot_sync(0xffffffffu, r == 1);
     if (__any_sync(0xffffffffu, r < 0) && lane == 0)
         atomicOr(a.status, kStatusTableOverflow);
-    if (fresh && lane == 0)
-        atomicAdd(&a.inst_unique[inst], (unsigned)__popc(fresh));
+    // New keys per instance, aggregated over the lanes sharing an instance.
+    const bool fresh = r == 1;
+    const unsigned peers = __match_any_sync(0xffffffffu, fresh ? inst : 0xFFFFFFFFu);
+    if (fresh && lane == (unsigned)(__ffs(peers) - 1))
+        atomicAdd(&a.inst_unique[inst], (unsigned)__popc(peers));
 }
 
-// Expansion.  Every iteration of the warp loop performs exactly one step of
-// each lane's depth-first walk -- test one candidate placement, descend,
-// backtrack, or complete the row -- so the lanes of a warp do uniform work;
-// a lane whose state is exhausted takes the next state of the CTA's chunk.
-// Completed rows are staged in shared memory and inserted by the whole warp,
-// 32 at a time.
+// Expansion.  Warps work independently (no block barrier): each warp takes
+// a chunk of work items from a global counter, and its lanes take items from
+// that chunk as they become free.  A work item is one state with its first
+// placement fixed (the state's walk split `fan` ways), so a state with
+// thousands of row fills spreads over many lanes.  Every iteration of the
+// warp loop performs exactly one step of each lane's depth-first walk --
+// test one candidate placement, descend, backtrack, or complete the row --
+// so the lanes do uniform work.  Placement tables are read through L1 from
+// global memory; each lane keeps its own instance, so a warp may move to a
+// chunk of another instance while some lanes finish earlier items.
+// Completed rows are staged in shared memory and inserted by the whole
+// warp, 32 at a time.
 template <bool K64>
 __global__ void __launch_bounds__(kExpandBlock)
 k_expand(ExpandArgs a) {
-    __shared__ SmemTable st;
     __shared__ WarpStage stage[kWarps];
-    __shared__ Seg s_seg;
-    __shared__ unsigned long long s_ci;
-    __shared__ unsigned int s_next;
-    uint32_t loaded = 0xFFFFFFFFu;
-    unsigned long long raw = 0;
     const unsigned lane = threadIdx.x & 31u;
-    const unsigned warp = threadIdx.x >> 5;
-    WarpStage &ws = stage[warp];
+    WarpStage &ws = stage[threadIdx.x >> 5];
     const unsigned lt_mask = (1u << lane) - 1u;
+    const uint32_t fan = a.fan ? a.fan : 1u;
+    unsigned long long raw = 0;
+
+    // Warp-uniform chunk cursor.
+    unsigned long long c_next = 0, c_end = 0;   // items of the current chunk not yet taken
+    uint32_t c_seg = 0;
+    bool no_more = false;
+
+    // Lane walk state and context.
+    bool active = false;
+    const Seg *sg = nullptr;
+    const InstDesc *d = nullptr;
+    const Plc *plc = nullptr;
+    uint32_t W = 0, rowmask = 0, dyn_bits = 0;
+    unsigned long long usedmask = 0, dynmask = 0;
+    unsigned long long w = 0, u = 0, cnt = 0, sidx = 0;
+    uint32_t scol = 0, depth = 0, idx = 0, min_depth = 0;
+    int nbuf = 0;   // warp-uniform: staged children
+
     for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            const unsigned long long ci = atomicAdd(a.work, 1ull);
-            s_ci = ci;
-            s_next = 0;
-            if (ci < a.n_chunks) {
+        // ---- hand out items to idle lanes ----------------------------------
+        unsigned need = __ballot_sync(0xffffffffu, !active);
+        while (need && !no_more) {
+            if (c_next >= c_end) {
+                unsigned long long ci = 0;
+                if (lane == 0)
+                    ci = atomicAdd(a.work, 1ull);
+                ci = __shfl_sync(0xffffffffu, ci, 0);
+                if (ci >= a.n_chunks) {
+                    no_more = true;
+                    break;
+                }
                 // Segment holding chunk ci: last seg with chunk_base <= ci.
                 uint32_t lo = 0, hi = a.n_segs - 1;
                 while (lo < hi) {
@@ -335,164 +364,181 @@ k_expand(ExpandArgs a) {
                     else
                         hi = mid - 1;
                 }
-                s_seg = a.segs[lo];
+                c_seg = lo;
+                const Seg &s = a.segs[lo];
+                c_next = s.begin + (ci - s.chunk_base) * a.chunk_states;
+                const unsigned long long se = s.begin + s.len;
+                c_end = c_next + a.chunk_states < se ? c_next + a.chunk_states : se;
             }
-        }
-        __syncthreads();
-        const unsigned long long ci = s_ci;
-        if (ci >= a.n_chunks)
-            break;
-        const Seg sg = s_seg;
-        if (sg.inst != loaded) {
-            load_table(st, a.insts + sg.inst, a.plc);
-            __syncthreads();
-            loaded = sg.inst;
-        }
-        const unsigned long long first = sg.begin + (ci - sg.chunk_base) * a.chunk_states;
-        const unsigned long long segend = sg.begin + sg.len;
-        const unsigned n_items = (unsigned)((first + a.chunk_states < segend ? first + a.chunk_states
-                                                                             : segend) -
-                                            first);
-        const uint32_t fan = a.fan;
-        const Codec cd = make_codec(st, sg.hi_board, sg.in_shift, sg.tag);
-        const uint32_t inst = sg.inst;
-        const uint32_t W = st.width;
-        const uint32_t rowmask = (1u << W) - 1u;
-
-        // Lane walk state.
-        bool active = false, exhausted = false;
-        unsigned long long w = 0, u = 0, cnt = 0, sidx = 0;
-        uint32_t scol = 0, depth = 0, idx = 0, min_depth = 0;
-        int nbuf = 0;   // warp-uniform: staged children
-        for (;;) {
-            if (!active && !exhausted) {
-                const unsigned i = atomicAdd(&s_next, 1u);
-                if (i < n_items) {
-                    const unsigned long long item = first + i;
-                    const unsigned long long si = fan ? item / fan : item;
-                    const ulonglong2 rec = a.recs[si];
-                    parse_key<K64>(cd, rec.x, rec.y, w, u);
-                    cnt = K64 ? rec.y : a.cnts[si];
-                    sidx = 0;
-                    scol = 0;
-                    depth = 0;
-                    idx = 0;
-                    active = true;
-                    if (fan) {
-                        // Split walk: place this item's first choice at the
-                        // root, then walk only beneath it (min_depth = 1).
-                        const uint32_t choice = (uint32_t)(item % fan);
-                        const uint32_t row = (uint32_t)w & rowmask;
-                        if (row == 0) {
-                            active = choice == 0;   // complete row: one item emits it
-                            min_depth = 0;
-                        } else {
-                            const uint32_t c = __ffs(row) - 1;
-                            active = false;
-                            if (choice < st.len[c]) {
-                                const uint32_t pi = st.off[c] + choice;
-                                const unsigned long long m = st.mask[pi];
-                                if (!(m & ~w)) {
-                                    const TypeField f = st.field[st.type[pi]];
-                                    if ((u & f.fm) < f.cap) {
-                                        sidx = choice;
-                                        scol = c;
-                                        depth = 1;
-                                        w &= ~m;
-                                        u += f.fm & (0ull - f.fm);
-                                        active = true;
-                                        min_depth = 1;
-                                    }
+            const unsigned long long avail = c_end - c_next;
+            const unsigned take = (unsigned)(avail < (unsigned long long)__popc(need)
+                                                 ? avail
+                                                 : (unsigned long long)__popc(need));
+            // The first `take` needing lanes (in lane order) get items.
+            const unsigned rank = __popc(need & lt_mask);
+            if (((need >> lane) & 1u) && rank < take) {
+                const unsigned long long item = c_next + rank;
+                sg = a.segs + c_seg;
+                d = a.insts + sg->inst;
+                plc = a.plc + d->plc_off;
+                W = d->width;
+                rowmask = (1u << W) - 1u;
+                dyn_bits = d->dyn_bits;
+                dynmask = (1ull << dyn_bits) - 1ull;
+                usedmask = (1ull << d->used_bits) - 1ull;
+                const unsigned long long si = item / fan;
+                const ulonglong2 rec = a.recs[si];
+                if constexpr (K64) {
+                    w = (rec.x & dynmask) | sg->hi_board;
+                    u = (rec.x >> dyn_bits) & usedmask;
+                    cnt = rec.y;
+                } else {
+                    w = rec.x;
+                    u = rec.y & kUsedMask128;
+                    cnt = a.cnts[si];
+                }
+                sidx = 0;
+                scol = 0;
+                depth = 0;
+                idx = 0;
+                min_depth = 0;
+                active = true;
+                if (a.fan) {
+                    // Place this item's first choice at the root, then walk
+                    // only beneath it (min_depth = 1).
+                    const uint32_t choice = (uint32_t)(item % fan);
+                    const uint32_t row = (uint32_t)w & rowmask;
+                    if (row == 0) {
+                        active = choice == 0;   // complete row: one item emits it
+                    } else {
+                        const uint32_t c = __ffs(row) - 1;
+                        active = false;
+                        if (choice < d->col_len[c]) {
+                            const Plc p = plc[d->col_off[c] + choice];
+                            if (!(p.mask & ~w)) {
+                                const TypeField f = d->types[p.type];
+                                if ((u & f.fm) < f.cap) {
+                                    sidx = choice;
+                                    scol = c;
+                                    depth = 1;
+                                    w &= ~p.mask;
+                                    u += f.fm & (0ull - f.fm);
+                                    active = true;
+                                    min_depth = 1;
                                 }
                             }
                         }
                     }
-                } else {
-                    exhausted = true;
                 }
             }
-            bool emit = false, pop = false;
-            unsigned long long ck0 = 0, ck1 = 0;
-            if (active) {
-                const uint32_t row = (uint32_t)w & rowmask;
-                if (row == 0) {
-                    // Row complete: the child, then back to the parent fill.
-                    emit = true;
-                    if constexpr (K64) {
-                        ck0 = cd.child64(w, u);
-                    } else {
-                        ck0 = (w >> W) | cd.in_shift;
-                        ck1 = u | cd.tag;
-                    }
-                    pop = true;
+            c_next += take;
+            need = __ballot_sync(0xffffffffu, !active);
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            if (no_more)
+                break;
+            continue;   // every item handed out was empty: hand out more
+        }
+
+        // ---- one walk step per lane -----------------------------------------
+        bool emit = false, pop = false;
+        unsigned long long ck0 = 0, ck1 = 0;
+        if (active) {
+            const uint32_t row = (uint32_t)w & rowmask;
+            if (row == 0) {
+                // Row complete: the child, then back to the parent fill.
+                emit = true;
+                if constexpr (K64) {
+                    ck0 = ((w >> W) & dynmask) | (u << dyn_bits) | sg->tag;
                 } else {
-                    const uint32_t c = __ffs(row) - 1;
-                    if (idx < st.len[c]) {
-                        const uint32_t pi = st.off[c] + idx;
-                        const unsigned long long m = st.mask[pi];
-                        bool take = !(m & ~w);
-                        TypeField f;
-                        if (take) {
-                            f = st.field[st.type[pi]];
-                            take = (u & f.fm) < f.cap;
-                        }
-                        if (take) {
-                            sidx |= (unsigned long long)idx << (8 * depth);
-                            scol |= c << (4 * depth);
-                            ++depth;
-                            w &= ~m;
-                            u += f.fm & (0ull - f.fm);
-                            idx = 0;
-                        } else {
-                            ++idx;
-                        }
-                    } else {
-                        pop = true;
+                    ck0 = (w >> W) | sg->in_shift;
+                    ck1 = u | sg->tag;
+                }
+                pop = true;
+            } else {
+                const uint32_t c = __ffs(row) - 1;
+                // Next candidate >= idx whose row-0 and row-1 cells fit:
+                // AND of the column's two filter bitsets.
+                const uint32_t fw = d->fwords;
+                const unsigned long long *f0 =
+                    a.filt + d->filt_off + d->f0_off[c] + (unsigned long long)(row >> (c + 1)) * fw;
+                const unsigned long long *f1 =
+                    a.filt + d->filt_off + d->f1_off[c] +
+                    (unsigned long long)((uint32_t)(w >> W) & rowmask) * fw;
+                bool found = false;
+                for (uint32_t k = idx >> 6; k < fw; ++k) {
+                    unsigned long long m = __ldg(f0 + k) & __ldg(f1 + k);
+                    if (k == (idx >> 6))
+                        m &= ~0ull << (idx & 63u);
+                    if (m) {
+                        idx = k * 64 + (uint32_t)(__ffsll((long long)m) - 1);
+                        found = true;
+                        break;
                     }
                 }
-                if (pop) {
-                    if (depth == min_depth) {
-                        active = false;
+                if (found) {
+                    const Plc p = plc[d->col_off[c] + idx];
+                    bool take = !(p.mask & ~w);
+                    TypeField f;
+                    if (take) {
+                        f = d->types[p.type];
+                        take = (u & f.fm) < f.cap;
+                    }
+                    if (take) {
+                        sidx |= (unsigned long long)idx << (8 * depth);
+                        scol |= c << (4 * depth);
+                        ++depth;
+                        w &= ~p.mask;
+                        u += f.fm & (0ull - f.fm);
+                        idx = 0;
                     } else {
-                        --depth;
-                        idx = (uint32_t)(sidx >> (8 * depth)) & 0xFFu;
-                        sidx &= ~(0xFFull << (8 * depth));
-                        const uint32_t c = (scol >> (4 * depth)) & 0xFu;
-                        scol &= ~(0xFu << (4 * depth));
-                        const uint32_t pi = st.off[c] + idx;
-                        w |= st.mask[pi];
-                        const unsigned long long fm = st.field[st.type[pi]].fm;
-                        u -= fm & (0ull - fm);
                         ++idx;
                     }
+                } else {
+                    pop = true;
                 }
             }
-            // Stage this iteration's children (<= 32) after the staged ones.
-            const unsigned em = __ballot_sync(0xffffffffu, emit);
-            if (emit) {
-                const int pos = nbuf + __popc(em & lt_mask);
-                ws.k0[pos] = ck0;
-                ws.k1[pos] = ck1;
-                ws.cnt[pos] = cnt;
-                ++raw;
+            if (pop) {
+                if (depth == min_depth) {
+                    active = false;
+                } else {
+                    --depth;
+                    idx = (uint32_t)(sidx >> (8 * depth)) & 0xFFu;
+                    sidx &= ~(0xFFull << (8 * depth));
+                    const uint32_t c = (scol >> (4 * depth)) & 0xFu;
+                    scol &= ~(0xFu << (4 * depth));
+                    const Plc p = plc[d->col_off[c] + idx];
+                    w |= p.mask;
+                    const unsigned long long fm = d->types[p.type].fm;
+                    u -= fm & (0ull - fm);
+                    ++idx;
+                }
             }
-            nbuf += __popc(em);
-            if (nbuf >= 32) {
-                __syncwarp();
-                flush_children<K64>(a, ws, nbuf - 32, 32, inst, lane);
-                nbuf -= 32;
-                __syncwarp();
-            }
-            if (__all_sync(0xffffffffu, !active && exhausted))
-                break;
         }
-        if (nbuf > 0) {
+        // ---- stage this iteration's children (<= 32) after the staged ones --
+        const unsigned em = __ballot_sync(0xffffffffu, emit);
+        if (emit) {
+            const int pos = nbuf + __popc(em & lt_mask);
+            ws.k0[pos] = ck0;
+            ws.k1[pos] = ck1;
+            ws.cnt[pos] = cnt;
+            ws.inst[pos] = sg->inst;
+            ++raw;
+        }
+        nbuf += __popc(em);
+        if (nbuf >= 32) {
             __syncwarp();
-            flush_children<K64>(a, ws, 0, nbuf, inst, lane);
+            flush_children<K64>(a, ws, nbuf - 32, 32, lane);
+            nbuf -= 32;
             __syncwarp();
         }
     }
-    // Reconverged here: one atomic per warp for the raw-children counter.
+    if (nbuf > 0) {
+        __syncwarp();
+        flush_children<K64>(a, ws, 0, nbuf, lane);
+        __syncwarp();
+    }
+    // One atomic per warp for the raw-children counter.
     unsigned long long tot = raw;
     for (int o = 16; o > 0; o >>= 1)
         tot += __shfl_down_sync(0xffffffffu, tot, o);

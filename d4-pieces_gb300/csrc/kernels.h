@@ -21,6 +21,7 @@ struct ExpandArgs {
                                      // (work item = state * fan + first choice)
     const InstDesc *insts;
     const Plc *plc;
+    const unsigned long long *filt;  // candidate filter bitsets (InstDesc::filt_off)
     const ulonglong2 *recs;          // frontier (K64 records / K128 keys)
     const unsigned long long *cnts;  // K128 counts
     void *table;                     // Slot16[cap] (K64) or Slot32[cap] (K128)

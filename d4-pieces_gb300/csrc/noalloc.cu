@@ -53,8 +53,12 @@ unsigned char *scratch_address(int dev) {
 
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// Largest candidate-filter block of one instance: (2^W - 1 + W * 2^W)
+// bitsets of up to 4 words for W = 8.
+constexpr size_t kMaxFilterWords = (255 + 8 * 256) * 4;
+
 struct Layout {
-    size_t desc, seg, misc, plc, front[2], cnts[2], table;
+    size_t desc, seg, misc, plc, filt, front[2], cnts[2], table;
     uint64_t cap_states, cap_slots;
 };
 
@@ -71,6 +75,8 @@ Layout make_layout(bool k64) {
     off = align256(off + 256);
     L.plc = off;
     off = align256(off + sizeof(Plc) * kMaxPlc);
+    L.filt = off;
+    off = align256(off + sizeof(unsigned long long) * kMaxFilterWords);
     const size_t rec = 16, cntb = k64 ? 0 : 8, slot = k64 ? 16 : 32;
     const size_t per_state = 2 * (rec + cntb) + 2 * slot;
     const uint64_t n = (kNoAllocScratchBytes - off - 4 * 256) / per_state;
@@ -119,6 +125,12 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
         d.win_rows = 64 / W;
         d.n_plc = (uint32_t)lib.plc.size();
         d.plc_off = 0;
+        d.filt_off = 0;
+        d.fwords = lib.fwords;
+        for (int c = 0; c < kMaxWidth; c++) {
+            d.f0_off[c] = lib.f0_off[c];
+            d.f1_off[c] = lib.f1_off[c];
+        }
         d.n_types = (uint32_t)lib.fields.size();
         d.dyn_bits = lib.dyn_bits;
         d.used_bits = lib.used_bits;
@@ -144,6 +156,7 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
         unsigned long long *d_cursor = d_raw + 2;
         unsigned long long *d_result = d_raw + 3;
         Plc *d_plc = reinterpret_cast<Plc *>(base + L.plc);
+        unsigned long long *d_filt = reinterpret_cast<unsigned long long *>(base + L.filt);
         ulonglong2 *d_front[2] = {reinterpret_cast<ulonglong2 *>(base + L.front[0]),
                                   reinterpret_cast<ulonglong2 *>(base + L.front[1])};
         unsigned long long *d_cnts[2] = {
@@ -157,6 +170,11 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
         cuda_check(cudaMemcpyAsync(d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, s), "upload");
         if (!lib.plc.empty())
             cuda_check(cudaMemcpyAsync(d_plc, lib.plc.data(), lib.plc.size() * sizeof(Plc),
+                                       cudaMemcpyHostToDevice, s),
+                       "upload");
+        if (!lib.filters.empty())
+            cuda_check(cudaMemcpyAsync(d_filt, lib.filters.data(),
+                                       lib.filters.size() * sizeof(unsigned long long),
                                        cudaMemcpyHostToDevice, s),
                        "upload");
         cuda_check(cudaMemsetAsync(base + L.misc, 0, 256, s), "memset");
@@ -200,10 +218,11 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
                     hi |= (unsigned long long)inst->rows[row + i] << (i * W);
             sg.hi_board = hi;
             sg.tag = tag;
-            const uint32_t fan = n * 4 < slots * 256 ? fan_max : 0;
+            const uint32_t fan = n * 4 < slots * 256 && fan_max > 1 ? fan_max : 0;
             const uint64_t items = n * (fan ? fan : 1);
-            uint64_t chunk = (items + 4 * slots - 1) / (4 * slots);
-            chunk = std::min<uint64_t>(std::max<uint64_t>((chunk + 63) / 64 * 64, 64), 4096);
+            const uint64_t warps = slots * 8;
+            uint64_t chunk = (items + 8 * warps - 1) / (8 * warps);
+            chunk = std::min<uint64_t>(std::max<uint64_t>((chunk + 31) / 32 * 32, 32), 1024);
             sg.begin = 0;
             sg.len = items;
             sg.chunk_base = 0;
@@ -220,6 +239,7 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
             a.fan = fan;
             a.insts = d_desc;
             a.plc = d_plc;
+            a.filt = d_filt;
             a.recs = d_front[cur];
             a.cnts = d_cnts[cur];
             a.table = d_table;
