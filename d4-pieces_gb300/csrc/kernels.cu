@@ -340,6 +340,7 @@ k_expand(ExpandArgs a) {
     unsigned long long usedmask = 0, dynmask = 0;
     unsigned long long w = 0, u = 0, cnt = 0, sidx = 0;
     uint32_t scol = 0, depth = 0, idx = 0, min_depth = 0;
+    unsigned long long rw = 0, ru = 0;   // walk state at the root of the lane's subtree
     int nbuf = 0;   // warp-uniform: staged children
 
     for (;;) {
@@ -430,6 +431,8 @@ k_expand(ExpandArgs a) {
                         }
                     }
                 }
+                rw = w;
+                ru = u;
             }
             c_next += take;
             need = __ballot_sync(0xffffffffu, !active);
@@ -438,6 +441,61 @@ k_expand(ExpandArgs a) {
             if (no_more)
                 break;
             continue;   // every item handed out was empty: hand out more
+        }
+        // ---- work donation: no items left, some lanes idle ------------------
+        // A lane that has descended below its subtree root gives the rest of
+        // the root node (candidates after its current root choice) to an
+        // idle lane and keeps only the subtree of that choice.
+        if (no_more) {
+            const unsigned idle = __ballot_sync(0xffffffffu, !active);
+            const unsigned donors = __ballot_sync(0xffffffffu, active && depth > min_depth);
+            if (idle && donors) {
+                const unsigned pairs = min(__popc(idle), __popc(donors));
+                const unsigned irank = __popc(idle & lt_mask);
+                const unsigned drank = __popc(donors & lt_mask);
+                const bool recv = !active && irank < pairs;
+                const bool give = active && depth > min_depth && drank < pairs;
+                const int src = recv ? (int)__fns(donors, 0, (int)irank + 1) : (int)lane;
+                // Donor's root choice and the start of the donated range.
+                uint32_t ci = 0, cc = 0;
+                if (give) {
+                    ci = (uint32_t)(sidx >> (8 * min_depth)) & 0xFFu;
+                    cc = (scol >> (4 * min_depth)) & 0xFu;
+                }
+                const unsigned long long d_rw = __shfl_sync(0xffffffffu, rw, src);
+                const unsigned long long d_ru = __shfl_sync(0xffffffffu, ru, src);
+                const unsigned long long d_cnt = __shfl_sync(0xffffffffu, cnt, src);
+                const uint32_t d_idx = __shfl_sync(0xffffffffu, ci + 1, src);
+                const unsigned long long d_sg =
+                    __shfl_sync(0xffffffffu, (unsigned long long)sg, src);
+                if (recv) {
+                    sg = reinterpret_cast<const Seg *>(d_sg);
+                    d = a.insts + sg->inst;
+                    plc = a.plc + d->plc_off;
+                    W = d->width;
+                    rowmask = (1u << W) - 1u;
+                    dyn_bits = d->dyn_bits;
+                    dynmask = (1ull << dyn_bits) - 1ull;
+                    usedmask = (1ull << d->used_bits) - 1ull;
+                    w = rw = d_rw;
+                    u = ru = d_ru;
+                    cnt = d_cnt;
+                    sidx = 0;
+                    scol = 0;
+                    depth = 0;
+                    min_depth = 0;
+                    idx = d_idx;
+                    active = true;
+                }
+                if (give) {
+                    // New subtree root: the old root with its choice placed.
+                    const Plc p = plc[d->col_off[cc] + ci];
+                    rw &= ~p.mask;
+                    const unsigned long long fm = d->types[p.type].fm;
+                    ru += fm & (0ull - fm);
+                    ++min_depth;
+                }
+            }
         }
 
         // ---- one walk step per lane -----------------------------------------
