@@ -613,11 +613,46 @@ int32_t or_rowdp(const or_problem *p, int32_t threads, double max_seconds,
                 pthread_join(th[w], NULL);
         }
         if (abort_flag) {
-            /* partial level: count the states expanded, drop their children */
+            /* Interrupted level.  Count the states expanded and drop their
+             * children; with time left (the memory cap stopped it), keep
+             * sampling the rest of the level in batches small enough for the
+             * cap, each expanded and de-duplicated, until the deadline. */
+            size_t pos = 0;
             for (int w = 0; w < T; w++) {
                 tot += jobs[w].expanded;
                 for (int s = 0; s < T; s++)
                     shards[w][s].n = 0;
+            }
+            for (int w = 0; w < T; w++)
+                pos += jobs[w].expanded;
+            size_t batch = pos / 4 + (size_t)T;
+            while (max_seconds > 0 && now_s() < t0 + max_seconds && batch) {
+                abort_flag = 0;
+                size_t lo = pos % cur.n, hi = lo + batch < cur.n ? lo + batch : cur.n;
+                for (int w = 0; w < T; w++) {
+                    jobs[w].lo = lo + (hi - lo) * (size_t)w / (size_t)T;
+                    jobs[w].hi = lo + (hi - lo) * (size_t)(w + 1) / (size_t)T;
+                }
+                for (int w = 0; w < T; w++)
+                    pthread_create(&th[w], NULL, dp_expand_worker, &jobs[w]);
+                for (int w = 0; w < T; w++)
+                    pthread_join(th[w], NULL);
+                size_t got = 0;
+                for (int w = 0; w < T; w++)
+                    got += jobs[w].expanded;
+                if (!abort_flag) {
+                    for (int w = 0; w < T; w++)
+                        pthread_create(&th[w], NULL, dp_merge_worker, &jobs[w]);
+                    for (int w = 0; w < T; w++)
+                        pthread_join(th[w], NULL);
+                } else {
+                    batch /= 2;
+                }
+                for (int w = 0; w < T; w++)
+                    for (int s = 0; s < T; s++)
+                        shards[w][s].n = 0;
+                tot += got;
+                pos = hi;
             }
             break;
         }

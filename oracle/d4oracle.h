@@ -68,10 +68,12 @@ void or_canonical_grid(const or_problem *p, const int8_t *grid, int8_t *out);
  * after completing row r (r = 0..H-1).  *count = number of tilings (mod
  * 2^64).  threads >= 1.  max_seconds > 0 stops once the elapsed time passes
  * the budget and max_children > 0 once a level's children exceed it (host
- * memory bound), both in the middle of a level if need be.  *levels_done
- * reports how many rows were completed and *states_total how many frontier
- * states were expanded (whole rows plus the expanded part of an interrupted
- * row).
+ * memory bound), both in the middle of a level if need be; when the cap
+ * stops a level with time left, the rest of that level is sampled in
+ * memory-bounded batches (expanded and de-duplicated, then dropped) until
+ * the budget is spent.  *levels_done reports how many rows were completed
+ * and *states_total how many frontier states were expanded (whole rows plus
+ * the expanded part of the interrupted row).
  * Returns 0 on success, -1 on bad input. */
 int32_t or_rowdp(const or_problem *p, int32_t threads, double max_seconds,
                  uint64_t max_children, uint64_t *level_sizes, uint64_t *count,
