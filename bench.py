@@ -47,9 +47,16 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--seed", type=int, default=SINGLE_LARGE_SEED)
-    ap.add_argument("--workload", choices=("single_large", "medium"), default="single_large",
+    ap.add_argument("--workload", choices=("single_large", "medium", "batched", "batched_one"),
+                    default="single_large",
                     help="medium = 8x10 board, 78 cells, 16 pieces (profiling case: frontier "
                          "of ~18M states, a few hundred MB -- larger than L2, a few GB at most)")
+    ap.add_argument("--instances", type=int, default=1024,
+                    help="batched workload: number of mix instances (seeded)")
+    ap.add_argument("--max-states", type=int, default=20_000_000,
+                    help="batched workloads: per-instance limit on one row's frontier")
+    ap.add_argument("--beam", type=int, default=256,
+                    help="batched solve-one: first sampled-frontier width")
     ap.add_argument("--cpu-budget", type=float, default=15.0,
                     help="seconds of host CPU work for the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -387,12 +394,75 @@ def bench_reference(args, dist: Dist) -> None:
     }), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# batched mix: all puzzles in one batch vs one puzzle at a time
+# ---------------------------------------------------------------------------
+BATCHED_SEED = 2024
+
+
+def bench_batched(args, dist: Dist) -> None:
+    """Batched mix: the same seeded instances once as one batch (one k_expand
+    + k_compact pair per board row for all of them) and once through the
+    plain path (one puzzle at a time).  Both runs apply the same per-instance
+    frontier limit; the counts (or solve-one outcomes) must agree."""
+    from d4gb import engine as E
+    from d4gb.problem import batched_mix, verify_tiling
+
+    probs = batched_mix(BATCHED_SEED, args.instances)
+    mode = E.MODE_SOLVE_ONE if args.workload == "batched_one" else E.MODE_COUNT
+    res = {}
+    outs = {}
+    for arm, seq in (("batched", False), ("plain", True)):
+        t0 = time.perf_counter()
+        out, st = E.batch_run(probs, mode=mode, sequential=seq, device=dist.local_rank,
+                              max_states=args.max_states, beam=args.beam)
+        wall = time.perf_counter() - t0
+        ok = [r for r in out if r["status"] == 0]
+        outs[arm] = out
+        res[arm] = {"wall_s": wall, "puzzles_per_s": len(probs) / wall,
+                    "states_per_s": st["states_out"] / wall,
+                    "completed": len(ok), "over_limit": len(out) - len(ok),
+                    "expand_launches": st["expand_launches"],
+                    "compact_launches": st["compact_launches"],
+                    "other_launches": st["other_launches"],
+                    "states": st["states_out"], "expand_ms": st["expand_ms"],
+                    "compact_ms": st["compact_ms"], "paused": st["paused"],
+                    "restarts": st["restarts"]}
+    for a, b in zip(outs["batched"], outs["plain"]):
+        if (a["status"], a["count"]) != (b["status"], b["count"]):
+            raise RuntimeError("batched and plain results differ")
+    extra = {}
+    if mode == E.MODE_SOLVE_ONE:
+        bad = sum(1 for p, r in zip(probs, outs["batched"])
+                  if r["found"] and not verify_tiling(p, r["grid"], r["steps"]))
+        if bad:
+            raise RuntimeError(f"{bad} solve-one tilings fail the cover check")
+        extra["found"] = sum(1 for r in outs["batched"] if r["found"])
+        extra["cover_checked"] = extra["found"]
+    if dist.rank == 0:
+        what = "solve-one" if mode == E.MODE_SOLVE_ONE else "solve-all counts"
+        print(json.dumps({
+            "metric": f"puzzles/s (batched mix, {what})",
+            "value": res["batched"]["puzzles_per_s"],
+            "unit": "puzzles/s",
+            "n_gpus": dist.world,
+            "config": {"workload": f"batched mix: {len(probs)} instances, seed {BATCHED_SEED}, "
+                                   "width 5-8, height 5-12, 0-4 holes, 3-6-cell pieces",
+                       "max_states_per_row": args.max_states, "beam": args.beam},
+            "batched": res["batched"], "plain": res["plain"],
+            "speedup_vs_plain": res["batched"]["puzzles_per_s"] / res["plain"]["puzzles_per_s"],
+            **extra,
+        }), flush=True)
+
+
 def main() -> None:
     args = parse_args()
     dist = Dist(args.gpus)
     try:
         if args.impl == "reference":
             bench_reference(args, dist)
+        elif args.workload in ("batched", "batched_one"):
+            bench_batched(args, dist)
         else:
             bench_ours(args, dist)
     finally:

@@ -1,6 +1,8 @@
 // abi.cu -- extern "C" boundary (include/d4e.h) over the engine.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -315,24 +317,33 @@ int d4e_searcher_level_sizes(const d4e_searcher *s, uint64_t *sizes, uint32_t ma
     });
 }
 
-static void fill_stats(const d4e::Engine &e, d4e_stats *st) {
+// Adds an engine's totals to *st (add = false: overwrites).
+static void fill_stats(const d4e::Engine &e, d4e_stats *st, bool add = false) {
     const d4e::Totals &t = e.totals();
-    st->rows = t.steps;
-    st->states_in = t.states_in;
-    st->states_raw = t.states_raw;
-    st->states_out = t.states_out;
-    st->peak_frontier = t.peak_frontier;
-    st->expand_launches = t.expand_launches;
-    st->compact_launches = t.compact_launches;
-    st->retries = t.retries;
-    st->other_launches = t.other_launches;
-    st->h2d_bytes = t.h2d_bytes;
-    st->d2h_bytes = t.d2h_bytes;
-    st->expand_ms = t.expand_ms;
-    st->compact_ms = t.compact_ms;
-    st->run_ms = t.run_ms;
-    st->record_bytes = e.packed_keys() ? 16 : 24;
-    st->slot_bytes = e.packed_keys() ? 16 : 32;
+    if (!add)
+        std::memset(st, 0, sizeof(*st));
+    st->rows += t.steps;
+    st->states_in += t.states_in;
+    st->states_raw += t.states_raw;
+    st->states_out += t.states_out;
+    st->peak_frontier = std::max<uint64_t>(st->peak_frontier, t.peak_frontier);
+    st->expand_launches += t.expand_launches;
+    st->compact_launches += t.compact_launches;
+    st->retries += t.retries;
+    st->other_launches += t.other_launches;
+    st->h2d_bytes += t.h2d_bytes;
+    st->d2h_bytes += t.d2h_bytes;
+    st->expand_ms += t.expand_ms;
+    st->compact_ms += t.compact_ms;
+    st->run_ms += t.run_ms;
+    if (!add || !st->record_bytes) {
+        st->record_bytes = e.packed_keys() ? 16 : 24;
+        st->slot_bytes = e.packed_keys() ? 16 : 32;
+    }
+    st->paused += t.paused;
+    st->splits += t.splits;
+    st->failed += t.failed;
+    st->restarts += t.restarts;
 }
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st) {
@@ -390,6 +401,147 @@ int d4e_batch_count(const d4e_instance *insts, uint32_t n, uint32_t flags, int32
         }
         if (st)
             fill_stats(eng, st);
+        return D4E_OK;
+    });
+}
+
+}  // extern "C"
+
+namespace {
+
+d4e::InstanceSpec to_spec(const d4e_instance &in, uint32_t mode, uint64_t max_states,
+                          uint64_t beam) {
+    d4e::InstanceSpec sp;
+    sp.width = in.width;
+    sp.height = in.height;
+    sp.rows = in.rows;
+    sp.shapes = in.shapes;
+    sp.counts = in.counts;
+    sp.n_pieces = in.n_pieces;
+    sp.sym = in.sym;
+    sp.mode = mode == D4E_MODE_SOLVE_ONE ? d4e::Mode::SolveOne : d4e::Mode::Count;
+    sp.max_states = max_states;
+    sp.beam = beam;
+    return sp;
+}
+
+uint32_t id_bits(uint32_t n) {
+    uint32_t b = 1;
+    while (b < 23 && (1ull << b) < n)
+        b++;
+    return b;
+}
+
+}  // namespace
+
+namespace d4e {
+
+// Result of one finished engine instance.
+void engine_result(Engine &eng, uint32_t id, uint32_t mode, d4e_result *r) {
+    r->mode = mode;
+    r->status = eng.status(id);
+    r->rows = eng.row(id);
+    r->count = 0;
+    r->found = 0;
+    std::memset(r->grid, -1, sizeof(r->grid));
+    std::memset(r->steps, -1, sizeof(r->steps));
+    if (r->status)
+        return;
+    if (mode == D4E_MODE_SOLVE_ONE) {
+        const uint32_t cells = eng.width(id) * eng.height(id);
+        if (cells > sizeof(r->grid))
+            throw Error(kErrInvalid, "solve-one boards are limited to 512 cells");
+        r->found = eng.solution(id, r->grid, r->steps) ? 1u : 0u;
+        r->count = r->found;
+    } else {
+        r->count = eng.count(id);
+    }
+}
+
+}  // namespace d4e
+
+extern "C" {
+
+int d4e_batch_run(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
+                  d4e_result *results, d4e_stats *st) {
+    return guarded([&] {
+        if ((!insts && n) || (!results && n))
+            return fail(D4E_ERR_INVALID, "null pointer");
+        const d4e_batch_opts o = opts ? *opts : d4e_batch_opts{};
+        if (o.mode > D4E_MODE_SOLVE_ONE)
+            return fail(D4E_ERR_INVALID, "unknown mode");
+        for (uint32_t i = 0; i < n; i++)
+            if (insts[i].width * insts[i].height > sizeof(results[i].grid) && o.mode)
+                return fail(D4E_ERR_INVALID, "solve-one boards are limited to 512 cells");
+        const auto t0 = std::chrono::steady_clock::now();
+        auto finish = [&](d4e::Engine &eng, uint32_t id, uint32_t i) {
+            d4e::engine_result(eng, id, o.mode, &results[i]);
+            results[i].tag = i;
+            results[i].queued_ms = 0;
+            results[i].latency_ms =
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
+                    .count();
+        };
+        d4e::EngineOpts eo;
+        eo.device = o.device;
+        eo.memory_budget = o.memory_budget;
+        eo.isolate_failures = true;
+        if (o.flags & D4E_BATCH_WIDE_KEYS)
+            eo.key_mode = d4e::KeyMode::K128;
+        if (st)
+            std::memset(st, 0, sizeof(*st));
+        if (o.flags & D4E_BATCH_SEQUENTIAL) {
+            d4e::Engine eng(eo);
+            for (uint32_t i = 0; i < n; i++) {
+                const uint32_t id = eng.add(to_spec(insts[i], o.mode, o.max_states, o.beam));
+                eng.run();
+                finish(eng, id, i);
+                eng.release(id);
+            }
+            if (st)
+                fill_stats(eng, st);
+            return D4E_OK;
+        }
+        // Packed 64-bit keys for every instance that fits them, the general
+        // encoding for the rest (a second engine, run after the first).
+        std::vector<uint32_t> rest;
+        if (o.flags & D4E_BATCH_WIDE_KEYS) {
+            for (uint32_t i = 0; i < n; i++)
+                rest.push_back(i);
+        } else {
+            d4e::EngineOpts e64 = eo;
+            e64.k64_inst_bits = id_bits(n);
+            d4e::Engine eng(e64);
+            std::vector<std::pair<uint32_t, uint32_t>> ids;   // (engine id, index)
+            for (uint32_t i = 0; i < n; i++) {
+                try {
+                    ids.push_back({eng.add(to_spec(insts[i], o.mode, o.max_states, o.beam)), i});
+                } catch (const d4e::Error &err) {
+                    if (err.code != d4e::kErrUnsupported ||
+                        std::string(err.what()).find("packed key") == std::string::npos)
+                        throw;
+                    rest.push_back(i);
+                }
+            }
+            eng.run();
+            for (const auto &[id, i] : ids)
+                finish(eng, id, i);
+            if (st)
+                fill_stats(eng, st, true);
+        }
+        if (!rest.empty()) {
+            d4e::EngineOpts e128 = eo;
+            e128.key_mode = d4e::KeyMode::K128;
+            d4e::Engine eng(e128);
+            std::vector<uint32_t> ids;
+            for (uint32_t i : rest)
+                ids.push_back(eng.add(to_spec(insts[i], o.mode, o.max_states, o.beam)));
+            eng.run();
+            for (size_t k = 0; k < rest.size(); k++)
+                finish(eng, ids[k], rest[k]);
+            if (st)
+                fill_stats(eng, st, true);
+        }
         return D4E_OK;
     });
 }

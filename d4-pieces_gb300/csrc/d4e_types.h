@@ -64,6 +64,7 @@ struct InstDesc {
     uint32_t n_types;
     uint32_t dyn_bits;    // width * (max piece rows - 1): window bits a K64 key keeps
     uint32_t used_bits;
+    uint32_t flags;       // kInstWitness: records carry a parent witness, not a count
     uint16_t col_off[kMaxWidth];   // placements anchored at column c: [col_off, col_off + col_len)
     uint16_t col_len[kMaxWidth];
     // Candidate filters (bitsets over a column's placements, `fwords` u64
@@ -79,6 +80,12 @@ struct InstDesc {
     TypeField types[kMaxTypes];
     uint8_t rows[kMaxHeight];      // board rows, bit c = cell to cover
 };
+
+// InstDesc::flags.  A solve-one instance's records carry, instead of a
+// count, the largest witness (instance-free key, see witness64/witness128 in
+// kernels.cu) of the parents that produce them, so that one tiling can be
+// traced back through its kept levels.
+constexpr uint32_t kInstWitness = 1u;
 
 // The frontier segment of one active instance.  It is cut into work chunks
 // of `chunk_states` states; chunk_base is the global index of its first chunk.
@@ -114,6 +121,8 @@ enum : uint32_t {
 // Cursor value marking an instance whose row being completed is its last:
 // its states are summed into the per-instance result instead of stored.
 constexpr unsigned long long kCursorFinal = ~0ull;
+// Cursor value of an instance whose children are discarded (it failed).
+constexpr unsigned long long kCursorDrop = ~0ull - 1ull;
 
 // Solution path node (one completed row of one partial tiling).
 struct PathNode {

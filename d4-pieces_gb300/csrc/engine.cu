@@ -21,9 +21,14 @@ template <class T>
 void DevBuf<T>::reserve(size_t n, cudaStream_t s, size_t keep) {
     if (n <= cap)
         return;
-    const size_t nc = std::max(n, cap + cap / 2);
+    size_t nc = std::max(n, cap + cap / 2);
     T *np = nullptr;
-    cuda_check(cudaMalloc(&np, nc * sizeof(T)), "cudaMalloc");
+    if (cudaMalloc(&np, nc * sizeof(T)) != cudaSuccess) {
+        // Geometric growth did not fit: take exactly what is needed.
+        cudaGetLastError();
+        nc = n;
+        cuda_check(cudaMalloc(&np, nc * sizeof(T)), "cudaMalloc");
+    }
     if (p) {
         if (keep)
             cuda_check(cudaMemcpyAsync(np, p, keep * sizeof(T), cudaMemcpyDeviceToDevice, s),
@@ -43,6 +48,10 @@ template struct DevBuf<Seg>;
 template struct DevBuf<ulonglong2>;
 template struct DevBuf<PathNode>;
 template struct DevBuf<unsigned char>;
+template struct DevBuf<CopyRange>;
+template struct DevBuf<TraceJob>;
+template struct DevBuf<LevelPtr>;
+template struct DevBuf<TraceOut>;
 
 namespace {
 
@@ -91,12 +100,35 @@ Engine::Engine(const EngineOpts &opts) : opts_(opts) {
     nraw_.reserve(2, stream_);
     if (opts_.chunk_states < 32)
         opts_.chunk_states = 32;
+    if (opts_.k64_inst_bits) {
+        if (opts_.k64_inst_bits > 23 || opts_.keep_levels)
+            throw Error(kErrInvalid, "k64_inst_bits must be 1..23 (and no keep_levels)");
+        k64_ = true;
+        inst_off_ = 63 - opts_.k64_inst_bits;
+        inst_mask_ = (1ull << opts_.k64_inst_bits) - 1ull;
+        mode_fixed_ = true;
+    }
 }
 
 Engine::~Engine() {
     DeviceGuard g(opts_.device);
     if (stream_)
         cudaStreamSynchronize(stream_);
+    for (auto &c : chunks_) {
+        if (c.keys)
+            cudaFreeAsync(c.keys, stream_);
+        if (c.cnts)
+            cudaFreeAsync(c.cnts, stream_);
+    }
+    if (stream_)
+        cudaStreamSynchronize(stream_);
+    if (pool_)
+        cudaMemPoolDestroy(pool_);
+    ranges_.release();
+    keep_max_.release();
+    jobs_.release();
+    lvlptr_.release();
+    trace_out_.release();
     for (auto p : lvl_keys_)
         cudaFree(p);
     for (auto p : lvl_cnts_)
@@ -154,16 +186,24 @@ uint32_t Engine::add(const InstanceSpec &sp) {
     if (inst_.size() >= kMaxInstances)
         throw Error(kErrUnsupported, "too many instances");
 
+    if (sp.mode == Mode::SolveOne && opts_.keep_levels)
+        throw Error(kErrInvalid, "solve-one instances need an engine without keep_levels");
+
     Inst in;
     const std::string err = build_piece_lib(sp.shapes, sp.counts, sp.n_pieces, sp.sym, sp.width,
                                             in.lib);
     if (!err.empty())
         throw Error(err.find("more than") != std::string::npos ? kErrUnsupported : kErrInvalid,
                     err);
-    const uint32_t id = (uint32_t)inst_.size();
-    if (mode_fixed_ && k64_ && n_active_ > 0 &&
+    const bool reuse = !free_ids_.empty();
+    const uint32_t id = reuse ? free_ids_.back() : (uint32_t)inst_.size();
+    const bool fixed_layout = opts_.k64_inst_bits != 0;
+    if (mode_fixed_ && k64_ && (n_active_ > 0 || fixed_layout) &&
         (in.lib.dyn_bits + in.lib.used_bits > inst_off_ || id > inst_mask_))
         throw Error(kErrUnsupported, "instance does not fit the engine's packed key layout");
+    in.mode = sp.mode;
+    in.limit = sp.max_states;
+    in.beam = sp.mode == Mode::SolveOne ? sp.beam : 0;
     in.width = sp.width;
     in.height = sp.height;
     InstDesc &d = in.desc;
@@ -197,18 +237,68 @@ uint32_t Engine::add(const InstanceSpec &sp) {
         w0 |= (unsigned long long)sp.rows[r] << (r * sp.width);
     in.root_window = w0;
 
-    ensure_inst_capacity(id + 1);
-    inst_.push_back(std::move(in));
+    d.flags = sp.mode == Mode::SolveOne ? kInstWitness : 0u;
+    if (reuse) {
+        free_ids_.pop_back();
+        inst_[id] = std::move(in);
+    } else {
+        ensure_inst_capacity(id + 1);
+        inst_.push_back(std::move(in));
+    }
     pending_.push_back(id);
     pending_upload_.push_back(id);
     return id;
+}
+
+void Engine::release(uint32_t id) {
+    Inst &in = inst_.at(id);
+    if (!in.done)
+        throw Error(kErrState, "instance has not finished");
+    if (!in.result_ready)
+        sync_results();
+    drop_levels(in);
+    in = Inst{};
+    in.done = true;
+    in.result_ready = true;
+    in.status = kErrState;
+    in.error = "instance released";
+    free_ids_.push_back(id);
+}
+
+void Engine::fail_instance(uint32_t id, int code, const std::string &msg) {
+    Inst &in = inst_[id];
+    in.status = code;
+    in.error = msg;
+    in.active = false;
+    in.done = true;
+    in.result = 0;
+    in.result_ready = true;
+    in.seg_len = 0;
+    drop_levels(in);
+    n_active_--;
+    tot_.failed++;
+}
+
+uint64_t Engine::frontier_bytes(int buf) const {
+    return (uint64_t)keys_[buf].cap * sizeof(ulonglong2) +
+           (uint64_t)cnts_[buf].cap * sizeof(unsigned long long);
+}
+
+double Engine::memory_limit(double device_avail) const {
+    // Bytes available to the next frontier and the table: what the device
+    // has, or what the budget leaves next to the current frontier.
+    if (!opts_.memory_budget)
+        return device_avail;
+    const double b = (double)opts_.memory_budget - (double)frontier_bytes(cur_) -
+                     (double)lvl_bytes_;
+    return std::min(device_avail, b);
 }
 
 void Engine::fix_key_mode() {
     // The encoding is chosen while no state is resident (first step, or any
     // step after every instance has finished), from the instances waiting to
     // start; later additions must fit it (checked in add()).
-    if (mode_fixed_ && (n_active_ > 0 || pending_.empty()))
+    if (opts_.k64_inst_bits || (mode_fixed_ && (n_active_ > 0 || pending_.empty())))
         return;
     uint32_t need = 0, max_id = 0;
     for (uint32_t id : pending_) {
@@ -228,21 +318,33 @@ void Engine::fix_key_mode() {
 void Engine::flush_uploads() {
     if (pending_upload_.empty())
         return;
-    // Descriptors and placement tables of newly added instances; ids are
-    // appended in order, so both land in one contiguous range.
-    const uint32_t lo = pending_upload_.front(), hi = pending_upload_.back() + 1;
+    // Descriptors of newly added instances, one copy per run of consecutive
+    // ids (ids are appended in order unless released ids are reused).
     std::vector<InstDesc> descs;
-    descs.reserve(hi - lo);
-    for (uint32_t id = lo; id < hi; id++)
+    descs.reserve(pending_upload_.size());
+    for (uint32_t id : pending_upload_)
         descs.push_back(inst_[id].desc);
-    cuda_check(cudaMemcpyAsync(insts_.p + lo, descs.data(), descs.size() * sizeof(InstDesc),
-                               cudaMemcpyHostToDevice, stream_),
-               "upload descriptors");
+    for (size_t i = 0; i < pending_upload_.size();) {
+        size_t j = i + 1;
+        while (j < pending_upload_.size() && pending_upload_[j] == pending_upload_[j - 1] + 1)
+            j++;
+        const uint32_t lo = pending_upload_[i];
+        cuda_check(cudaMemcpyAsync(insts_.p + lo, descs.data() + i, (j - i) * sizeof(InstDesc),
+                                   cudaMemcpyHostToDevice, stream_),
+                   "upload descriptors");
+        cuda_check(cudaMemsetAsync(results_.p + lo, 0, (j - i) * sizeof(unsigned long long),
+                                   stream_),
+                   "memset");
+        cuda_check(cudaMemsetAsync(final_states_.p + lo, 0, (j - i) * sizeof(unsigned int),
+                                   stream_),
+                   "memset");
+        i = j;
+    }
     tot_.h2d_bytes += descs.size() * sizeof(InstDesc);
-    // Placement tables are packed back to back in id order.
+    // Placement tables are packed back to back in order of addition.
     std::vector<Plc> plc;
     plc.reserve(plc_total_ - plc_uploaded_);
-    for (uint32_t id = lo; id < hi; id++) {
+    for (uint32_t id : pending_upload_) {
         const auto &v = inst_[id].lib.plc;
         plc.insert(plc.end(), v.begin(), v.end());
     }
@@ -255,7 +357,7 @@ void Engine::flush_uploads() {
     plc_uploaded_ = plc_total_;
     std::vector<unsigned long long> filt;
     filt.reserve(filt_total_ - filt_uploaded_);
-    for (uint32_t id = lo; id < hi; id++) {
+    for (uint32_t id : pending_upload_) {
         const auto &v = inst_[id].lib.filters;
         filt.insert(filt.end(), v.begin(), v.end());
     }
@@ -267,13 +369,27 @@ void Engine::flush_uploads() {
                    "upload filters");
     tot_.h2d_bytes += filt.size() * sizeof(unsigned long long);
     filt_uploaded_ = filt_total_;
-    cuda_check(cudaMemsetAsync(results_.p + lo, 0, (hi - lo) * sizeof(unsigned long long), stream_),
-               "memset");
-    cuda_check(cudaMemsetAsync(final_states_.p + lo, 0, (hi - lo) * sizeof(unsigned int), stream_),
-               "memset");
     // The host staging vectors die here: make sure the copies have read them.
     cuda_check(cudaStreamSynchronize(stream_), "upload tables");
     pending_upload_.clear();
+}
+
+uint64_t Engine::projected_bytes(uint32_t id) const {
+    const Inst &in = inst_.at(id);
+    if (in.done)
+        return 0;
+    const double per_state = (k64_ ? 16.0 : 24.0) + (double)(slot_units() * 16) / opts_.target_load;
+    const double est = (double)std::max<uint64_t>(in.seg_len, 1) * in.growth;
+    return (uint64_t)(est * per_state + (double)in.seg_len * (k64_ ? 16.0 : 24.0));
+}
+
+uint64_t Engine::peak_bytes(uint32_t id) const {
+    const Inst &in = inst_.at(id);
+    uint64_t peak = 1;
+    for (uint64_t v : in.level_sizes)
+        peak = std::max(peak, v);
+    const double per_state = (k64_ ? 16.0 : 24.0) + (double)(slot_units() * 16) / opts_.target_load;
+    return (uint64_t)((double)peak * per_state);
 }
 
 uint64_t Engine::next_size_estimate(uint32_t id) const {
@@ -327,11 +443,13 @@ uint64_t Engine::table_capacity(uint64_t want) {
         return want;
     size_t free_b = 0, total_b = 0;
     cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
-    const uint64_t rec_bytes = k64_ ? 16 : 24;
-    const uint64_t next_frontier = (uint64_t)((double)want * opts_.target_load) * rec_bytes;
-    const uint64_t avail = (uint64_t)table_.cap * sizeof(ulonglong2) + free_b;
-    const uint64_t keep = total_b / 10 + next_frontier;
-    const uint64_t limit = avail > keep ? (avail - keep) / slot_bytes : 0;
+    // Each slot is paired with room for load * rec_bytes of next frontier,
+    // so the bound does not depend on `want`.
+    const double rec_bytes = k64_ ? 16.0 : 24.0;
+    const double avail = memory_limit((double)table_.cap * sizeof(ulonglong2) + (double)free_b -
+                                      0.1 * (double)total_b);
+    const uint64_t limit =
+        avail > 0 ? (uint64_t)(avail / ((double)slot_bytes + opts_.target_load * rec_bytes)) : 0;
     return std::max<uint64_t>(std::min<uint64_t>(want, limit / 1024 * 1024), 1ull << 20);
 }
 
@@ -402,192 +520,380 @@ StepStats Engine::step() {
         // rk / rc are pageable: wait until the copies have read them.
         cuda_check(cudaStreamSynchronize(stream_), "upload roots");
         n_cur_ += rk.size();
+        std::vector<uint32_t> roots;
+        for (uint32_t id : pending_)
+            if (inst_[id].mode == Mode::SolveOne)
+                roots.push_back(id);
         pending_.clear();
+        keep_levels_of(roots);   // level 0 of solve-one instances
     }
     if (n_active_ == 0)
         return st;
 
-    // Segments of the active instances, in frontier order.
+    // Active instances in frontier order.
     std::sort(active_.begin(), active_.end(),
               [&](uint32_t a, uint32_t b) { return inst_[a].seg_begin < inst_[b].seg_begin; });
-    // A state's walk can be cut by its first placement into `fan` work items
-    // (fan = the longest placement list of a column), so a handful of states
-    // still fills the GPU.
-    int occ = expand_occupancy();
+    const int occ = expand_occupancy();
     const uint64_t slots = (uint64_t)sms_ * (uint64_t)occ;
-    // Only frontiers with fewer states than a quarter of the resident lanes
-    // are split; larger ones already fill the GPU, and warps fetch chunks
-    // independently, so a heavy state delays only its own lane.
-    uint32_t fan = 0;
-    if (n_cur_ * 4 < slots * 256)
-        for (uint32_t id : active_)
-            for (int c = 0; c < kMaxWidth; c++)
-                fan = std::max<uint32_t>(fan, inst_[id].desc.col_len[c]);
-    if (fan <= 1)
-        fan = 0;
-    const uint64_t items = n_cur_ * (fan ? fan : 1);
-    // Warps take chunks independently: about eight chunks per resident warp,
-    // within [32, chunk_states] items.
-    const uint64_t warps = slots * 8;
-    uint64_t chunk = (items + 8 * warps - 1) / (8 * warps);
-    chunk = std::min<uint64_t>(std::max<uint64_t>(round_up(chunk, 32), 32), opts_.chunk_states);
-    std::vector<Seg> segs;
-    segs.reserve(active_.size());
-    uint64_t n_chunks = 0;
-    const uint64_t per = fan ? fan : 1;
-    for (uint32_t id : active_) {
-        const Inst &in = inst_[id];
-        Seg s = seg_for(id, in.row);
-        s.begin = in.seg_begin * per;
-        s.len = in.seg_len * per;
-        s.chunk_base = n_chunks;
-        n_chunks += (s.len + chunk - 1) / chunk;
-        segs.push_back(s);
-    }
-    segs_.reserve(segs.size(), stream_);
-    cuda_check(cudaMemcpyAsync(segs_.p, segs.data(), segs.size() * sizeof(Seg),
-                               cudaMemcpyHostToDevice, stream_),
-               "upload segments");
-    tot_.h2d_bytes += segs.size() * sizeof(Seg);
-
-    st.n_in = n_cur_;
-    const uint64_t est = (uint64_t)((double)std::max<uint64_t>(n_cur_, 1) * growth_ /
-                                    opts_.target_load);
-    uint64_t cap = table_capacity(est);
     const size_t n_inst = inst_.size();
     h_unique_.assign(n_inst, 0);
-    unsigned int h_status = 0;
-    unsigned long long h_raw = 0;
-    for (;;) {
-        const uint64_t units = cap * slot_units();
-        if (table_.cap < units) {
-            table_.release();
-            table_clean_ = 0;
-            table_.reserve(units, stream_);
-        }
-        if (table_clean_ < units) {
-            cuda_check(cudaMemsetAsync(table_.p + table_clean_, 0,
-                                       (units - table_clean_) * sizeof(ulonglong2), stream_),
-                       "memset table");
-            table_clean_ = units;
-        }
-        cuda_check(cudaMemsetAsync(inst_unique_.p, 0, n_inst * sizeof(unsigned int), stream_),
-                   "memset");
-        cuda_check(cudaMemsetAsync(misc_.p, 0, 4 * sizeof(unsigned int), stream_), "memset");
-        cuda_check(cudaMemsetAsync(nraw_.p, 0, 2 * sizeof(unsigned long long), stream_), "memset");
-        ExpandArgs a;
-        a.segs = segs_.p;
-        a.n_segs = (uint32_t)segs.size();
-        a.n_chunks = n_chunks;
-        a.chunk_states = chunk;
-        a.fan = fan;
-        a.insts = insts_.p;
-        a.plc = plc_.p;
-        a.filt = filt_.p;
-        a.recs = keys_[cur_].p;
-        a.cnts = cnts_[cur_].p;
-        a.table = table_.p;
-        a.cap = cap;
-        a.inst_unique = inst_unique_.p;
-        a.n_raw = nraw_.p;
-        a.status = misc_.p;
-        a.work = nraw_.p + 1;
-        a.max_probe = opts_.max_probe;
-        const int grid = (int)std::min<uint64_t>(n_chunks, (uint64_t)sms_ * (uint64_t)occ);
-        cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
-        launch_expand(k64_, a, grid, stream_);
-        cuda_check(cudaGetLastError(), "k_expand launch");
-        cuda_check(cudaEventRecord(ev_[1], stream_), "cudaEventRecord");
-        tot_.expand_launches++;
-        cuda_check(cudaMemcpyAsync(&h_status, misc_.p, sizeof(unsigned int),
-                                   cudaMemcpyDeviceToHost, stream_),
-                   "read status");
-        cuda_check(cudaMemcpyAsync(&h_raw, nraw_.p, sizeof(unsigned long long),
-                                   cudaMemcpyDeviceToHost, stream_),
-                   "read raw");
-        cuda_check(cudaMemcpyAsync(h_unique_.data(), inst_unique_.p, n_inst * sizeof(unsigned int),
-                                   cudaMemcpyDeviceToHost, stream_),
-                   "read unique");
-        cuda_check(cudaStreamSynchronize(stream_), "k_expand");
-        tot_.d2h_bytes += sizeof(unsigned int) + sizeof(unsigned long long) +
-                          n_inst * sizeof(unsigned int);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
-        st.expand_ms += ms;
-        if (!(h_status & kStatusTableOverflow))
-            break;
-        // Table too small for this row: clear it, grow it, redo the row.
-        cuda_check(cudaMemsetAsync(table_.p, 0, units * sizeof(ulonglong2), stream_),
-                   "memset table");
-        // Every child was produced (h_raw), so raw / load slots cannot
-        // overflow again; the memory cap applies.
-        const uint64_t want =
-            std::max<uint64_t>(cap * 8, (uint64_t)((double)h_raw / opts_.target_load));
-        const uint64_t grown = table_capacity(want);
-        if (grown <= cap)
-            throw Error(kErrNoMem, "hash table cannot grow: device memory exhausted");
-        cap = grown;
-        st.retries++;
-        tot_.retries++;
+    h_cursor_.assign(n_inst, 0ull);
+    st.n_in = n_cur_;
+
+    // Which instances run this row.  The next frontier must hold the
+    // projected children of the running instances plus the unchanged
+    // segments of the paused ones, next to the current frontier and a hash
+    // table; instances that do not fit wait (their states are carried over
+    // unchanged) and run once memory frees up.  Older instances go first and
+    // the oldest always runs.
+    const uint64_t slot_bytes = slot_units() * sizeof(ulonglong2);
+    const double rec_bytes = k64_ ? 16.0 : 24.0;
+    const int nxt_buf = 1 - cur_;
+    double mem = 0;
+    {
+        size_t free_b = 0, total_b = 0;
+        cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+        mem = memory_limit((double)free_b + (double)table_.cap * sizeof(ulonglong2) +
+                           (double)frontier_bytes(nxt_buf) - 0.1 * (double)total_b);
     }
-    st.n_raw = h_raw;
-    st.table_cap = cap;
-    if (opts_.max_frontier) {
+    std::vector<uint32_t> order(active_);
+    std::sort(order.begin(), order.end());
+    std::vector<uint32_t> run, paused;
+    double paused_bytes = 0, run_front = 0, run_table = 0;
+    for (uint32_t id : order)
+        paused_bytes += (double)inst_[id].seg_len * rec_bytes;
+    for (uint32_t id : order) {
+        const Inst &in = inst_[id];
+        const double est = (double)std::max<uint64_t>(in.seg_len, 1) * in.growth;
+        const double f = est * rec_bytes, t = est / opts_.target_load * (double)slot_bytes;
+        const double seg_b = (double)in.seg_len * rec_bytes;
+        const double need = run_front + f + (paused_bytes - seg_b) + std::max(run_table, t);
+        if (run.empty() || need <= mem) {
+            run.push_back(id);
+            run_front += f;
+            paused_bytes -= seg_b;
+            run_table = std::max(run_table, t);
+        } else {
+            paused.push_back(id);
+        }
+    }
+    std::sort(run.begin(), run.end(),
+              [&](uint32_t a, uint32_t b) { return inst_[a].seg_begin < inst_[b].seg_begin; });
+    st.paused = (uint32_t)paused.size();
+    st.n_in = 0;
+    for (uint32_t id : run)
+        st.n_in += inst_[id].seg_len;
+
+    // Split the running instances into groups whose estimated children fit
+    // the table budget; each group is one k_expand + k_compact pair.
+    // Usually one group holds them all.
+    const double table_mem = std::max(mem - run_front - paused_bytes, run_table);
+    const uint64_t budget_slots = (uint64_t)(table_mem / (double)slot_bytes);
+    std::vector<std::vector<uint32_t>> groups(1);
+    {
+        double acc = 0;
+        for (uint32_t id : run) {
+            const Inst &in = inst_[id];
+            const double e = (double)std::max<uint64_t>(in.seg_len, 1) * in.growth /
+                             opts_.target_load;
+            if (!groups.back().empty() && acc + e > (double)budget_slots) {
+                groups.emplace_back();
+                acc = 0;
+            }
+            groups.back().push_back(id);
+            acc += e;
+        }
+    }
+
+    uint64_t off = 0;                                     // next-frontier fill
+    std::vector<std::pair<uint32_t, uint64_t>> nseg;      // (id, begin)
+    std::vector<uint32_t> finishing;
+    const int nxt = 1 - cur_;
+    // Groups are processed from a work list: a group whose children overflow
+    // the largest table the device can hold is split in half and both halves
+    // are redone.
+    std::vector<std::vector<uint32_t>> work(groups.rbegin(), groups.rend());
+    while (!work.empty()) {
+        const std::vector<uint32_t> grp = std::move(work.back());
+        work.pop_back();
+        uint64_t n_grp = 0;
+        double est = 0;
+        for (uint32_t id : grp) {
+            n_grp += inst_[id].seg_len;
+            est += (double)std::max<uint64_t>(inst_[id].seg_len, 1) * inst_[id].growth;
+        }
+        // Small frontiers (fewer states than a quarter of the resident lanes)
+        // are split: each state's walk is cut by its first placement into
+        // `fan` work items (the longest placement list of a column), so a
+        // handful of states still fills the GPU.  Larger ones already do, and
+        // warps fetch chunks independently with in-warp work donation.
+        uint32_t fan = 0;
+        if (n_grp * 4 < slots * 256)
+            for (uint32_t id : grp)
+                for (int c = 0; c < kMaxWidth; c++)
+                    fan = std::max<uint32_t>(fan, inst_[id].desc.col_len[c]);
+        if (fan <= 1)
+            fan = 0;
+        const uint64_t per = fan ? fan : 1;
+        const uint64_t items = n_grp * per;
+        // Warps take chunks independently: about eight chunks per resident
+        // warp, within [32, chunk_states] items.
+        const uint64_t warps = slots * 8;
+        uint64_t chunk = (items + 8 * warps - 1) / (8 * warps);
+        chunk = std::min<uint64_t>(std::max<uint64_t>(round_up(chunk, 32), 32),
+                                   opts_.chunk_states);
+        std::vector<Seg> segs;
+        segs.reserve(grp.size());
+        uint64_t n_chunks = 0;
+        for (uint32_t id : grp) {
+            const Inst &in = inst_[id];
+            Seg s = seg_for(id, in.row);
+            s.begin = in.seg_begin * per;
+            s.len = in.seg_len * per;
+            s.chunk_base = n_chunks;
+            n_chunks += (s.len + chunk - 1) / chunk;
+            segs.push_back(s);
+        }
+        segs_.reserve(segs.size(), stream_);
+        cuda_check(cudaMemcpyAsync(segs_.p, segs.data(), segs.size() * sizeof(Seg),
+                                   cudaMemcpyHostToDevice, stream_),
+                   "upload segments");
+        tot_.h2d_bytes += segs.size() * sizeof(Seg);
+
+        uint64_t cap = table_capacity((uint64_t)(std::max(est, 1.0) / opts_.target_load));
+        unsigned int h_status = 0;
+        unsigned long long h_raw = 0;
+        bool split = false;
+        for (;;) {
+            const uint64_t units = cap * slot_units();
+            if (table_.cap < units) {
+                table_.release();
+                table_clean_ = 0;
+                table_.reserve(units, stream_);
+            }
+            if (table_clean_ < units) {
+                cuda_check(cudaMemsetAsync(table_.p + table_clean_, 0,
+                                           (units - table_clean_) * sizeof(ulonglong2), stream_),
+                           "memset table");
+                table_clean_ = units;
+            }
+            cuda_check(cudaMemsetAsync(inst_unique_.p, 0, n_inst * sizeof(unsigned int), stream_),
+                       "memset");
+            cuda_check(cudaMemsetAsync(misc_.p, 0, 4 * sizeof(unsigned int), stream_), "memset");
+            cuda_check(cudaMemsetAsync(nraw_.p, 0, 2 * sizeof(unsigned long long), stream_),
+                       "memset");
+            ExpandArgs a;
+            a.segs = segs_.p;
+            a.n_segs = (uint32_t)segs.size();
+            a.n_chunks = n_chunks;
+            a.chunk_states = chunk;
+            a.fan = fan;
+            a.insts = insts_.p;
+            a.plc = plc_.p;
+            a.filt = filt_.p;
+            a.recs = keys_[cur_].p;
+            a.cnts = cnts_[cur_].p;
+            a.table = table_.p;
+            a.cap = cap;
+            a.inst_unique = inst_unique_.p;
+            a.n_raw = nraw_.p;
+            a.status = misc_.p;
+            a.work = nraw_.p + 1;
+            a.max_probe = opts_.max_probe;
+            const int grid = (int)std::min<uint64_t>(n_chunks, slots);
+            cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
+            launch_expand(k64_, a, grid, stream_);
+            cuda_check(cudaGetLastError(), "k_expand launch");
+            cuda_check(cudaEventRecord(ev_[1], stream_), "cudaEventRecord");
+            tot_.expand_launches++;
+            cuda_check(cudaMemcpyAsync(&h_status, misc_.p, sizeof(unsigned int),
+                                       cudaMemcpyDeviceToHost, stream_),
+                       "read status");
+            cuda_check(cudaMemcpyAsync(&h_raw, nraw_.p, sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost, stream_),
+                       "read raw");
+            h_grp_unique_.resize(n_inst);
+            cuda_check(cudaMemcpyAsync(h_grp_unique_.data(), inst_unique_.p,
+                                       n_inst * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                       stream_),
+                       "read unique");
+            cuda_check(cudaStreamSynchronize(stream_), "k_expand");
+            tot_.d2h_bytes += sizeof(unsigned int) + sizeof(unsigned long long) +
+                              n_inst * sizeof(unsigned int);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
+            st.expand_ms += ms;
+            if (!(h_status & kStatusTableOverflow))
+                break;
+            // Table too small for this group: clear it, then grow it (up to
+            // raw / load slots, which cannot overflow again) or, when the
+            // device cannot hold that, split the group.
+            cuda_check(cudaMemsetAsync(table_.p, 0, units * sizeof(ulonglong2), stream_),
+                       "memset table");
+            st.retries++;
+            tot_.retries++;
+            const uint64_t want =
+                std::max<uint64_t>(cap * 4, (uint64_t)((double)h_raw / opts_.target_load));
+            const uint64_t grown = table_capacity(want);
+            if (grown >= want || (grp.size() == 1 && grown > cap)) {
+                cap = grown;
+                continue;
+            }
+            if (grp.size() == 1) {
+                if (!opts_.isolate_failures)
+                    throw Error(kErrNoMem, "hash table cannot grow: device memory exhausted");
+                fail_instance(grp[0], kErrNoMem,
+                              "row does not fit the device: " + std::to_string(h_raw) +
+                                  " children");
+                st.failed++;
+            } else {
+                const size_t half = grp.size() / 2;
+                work.emplace_back(grp.begin() + half, grp.end());
+                work.emplace_back(grp.begin(), grp.begin() + half);
+                tot_.splits++;
+            }
+            split = true;
+            break;
+        }
+        if (split)
+            continue;
+        st.groups++;
+        // Only this group's counters are valid in the read-back.
+        for (uint32_t id : grp)
+            h_unique_[id] = h_grp_unique_[id];
+        st.n_raw += h_raw;
+        st.table_cap = std::max<uint64_t>(st.table_cap, cap);
         uint64_t uniq = 0;
-        for (uint32_t id : active_)
+        for (uint32_t id : grp)
             uniq += h_unique_[id];
-        if (uniq > opts_.max_frontier) {
+        if (opts_.max_frontier && st.n_out + uniq > opts_.max_frontier) {
             cuda_check(cudaMemsetAsync(table_.p, 0, cap * slot_units() * sizeof(ulonglong2),
                                        stream_),
                        "memset table");
             cuda_check(cudaStreamSynchronize(stream_), "memset table");
-            throw Error(kErrUnsupported, "frontier limit exceeded: " + std::to_string(uniq) +
-                                             " states");
+            throw Error(kErrUnsupported, "frontier limit exceeded: " +
+                                             std::to_string(st.n_out + uniq) + " states");
         }
-    }
 
-    // Next segments: exclusive scan of the per-instance new-key counts.
-    h_cursor_.assign(n_inst, 0ull);
-    uint64_t off = 0;
-    std::vector<std::pair<uint32_t, uint64_t>> nseg;  // (id, begin)
-    std::vector<uint32_t> finishing;
-    for (uint32_t id : active_) {
-        const Inst &in = inst_[id];
-        const uint64_t u = h_unique_[id];
-        st.n_out += u;
-        if (in.row + 1 == in.height && !opts_.keep_levels) {
-            h_cursor_[id] = kCursorFinal;
-            finishing.push_back(id);
-        } else {
-            h_cursor_[id] = off;
-            nseg.push_back({id, off});
-            off += u;
+        // This group's next segments follow the previous groups' ones.
+        const uint64_t off0 = off;
+        for (uint32_t id : grp) {
+            const Inst &in = inst_[id];
+            const uint64_t u = h_unique_[id];
+            if (in.limit && u > in.limit) {
+                // Over its own frontier limit: the instance fails, its
+                // children are dropped by the compaction.
+                h_cursor_[id] = kCursorDrop;
+                fail_instance(id, kErrUnsupported,
+                              "frontier limit exceeded: " + std::to_string(u) + " states");
+                st.failed++;
+                continue;
+            }
+            st.n_out += u;
+            if (in.row + 1 == in.height && !opts_.keep_levels && in.mode == Mode::Count) {
+                h_cursor_[id] = kCursorFinal;
+                finishing.push_back(id);
+            } else {
+                h_cursor_[id] = off;
+                nseg.push_back({id, off});
+                off += u;
+            }
+        }
+        keys_[nxt].reserve(std::max<uint64_t>(off, 1), stream_, off0);
+        if (!k64_)
+            cnts_[nxt].reserve(std::max<uint64_t>(off, 1), stream_, off0);
+        cuda_check(cudaMemcpyAsync(cursor_.p, h_cursor_.data(),
+                                   n_inst * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                                   stream_),
+                   "upload cursors");
+        tot_.h2d_bytes += n_inst * sizeof(unsigned long long);
+        // Solve-one instances over their sample width keep a hash-chosen
+        // subset of about `beam` states (the same subset alone or batched).
+        std::vector<uint32_t> sampled;
+        for (uint32_t id : grp) {
+            Inst &in = inst_[id];
+            if (in.mode == Mode::SolveOne && in.beam && !in.done && h_unique_[id] > in.beam)
+                sampled.push_back(id);
+        }
+        if (!sampled.empty()) {
+            h_keep_max_.assign(n_inst, ~0ull);
+            for (uint32_t id : sampled) {
+                const double frac = (double)inst_[id].beam / (double)h_unique_[id];
+                h_keep_max_[id] = (unsigned long long)std::ldexp(frac, 64);
+                inst_[id].sampled = true;
+            }
+            keep_max_.reserve(n_inst, stream_);
+            cuda_check(cudaMemcpyAsync(keep_max_.p, h_keep_max_.data(),
+                                       n_inst * sizeof(unsigned long long),
+                                       cudaMemcpyHostToDevice, stream_),
+                       "upload sample thresholds");
+            tot_.h2d_bytes += n_inst * sizeof(unsigned long long);
+        }
+        CompactArgs c;
+        c.table = table_.p;
+        c.cap = cap;
+        c.cursor = cursor_.p;
+        c.out_recs = keys_[nxt].p;
+        c.out_cnts = cnts_[nxt].p;
+        c.results = results_.p;
+        c.final_states = final_states_.p;
+        c.inst_off = inst_off_;
+        c.inst_mask = inst_mask_;
+        c.keep_max = sampled.empty() ? nullptr : keep_max_.p;
+        const int cgrid = (int)std::min<uint64_t>((cap + 255) / 256, (uint64_t)sms_ * 8);
+        cuda_check(cudaEventRecord(ev_[2], stream_), "cudaEventRecord");
+        launch_compact(k64_, c, cgrid, stream_);
+        cuda_check(cudaGetLastError(), "k_compact launch");
+        cuda_check(cudaEventRecord(ev_[3], stream_), "cudaEventRecord");
+        tot_.compact_launches++;
+        cuda_check(cudaStreamSynchronize(stream_), "k_compact");
+        float cms = 0.f;
+        cudaEventElapsedTime(&cms, ev_[2], ev_[3]);
+        st.compact_ms += cms;
+        if (!sampled.empty()) {
+            // Kept states per sampled instance = cursor advance.
+            std::vector<unsigned long long> cend(n_inst);
+            cuda_check(cudaMemcpy(cend.data(), cursor_.p, n_inst * sizeof(unsigned long long),
+                                  cudaMemcpyDeviceToHost),
+                       "read cursors");
+            tot_.d2h_bytes += n_inst * sizeof(unsigned long long);
+            for (uint32_t id : sampled)
+                h_unique_[id] = (unsigned int)(cend[id] - h_cursor_[id]);
+        }
+        // Per-instance growth estimates for the next row.
+        for (uint32_t id : grp) {
+            Inst &in = inst_[id];
+            if (in.seg_len)
+                in.growth = std::clamp((double)h_unique_[id] / (double)in.seg_len * 1.25, 1.0,
+                                       256.0);
         }
     }
-    const int nxt = 1 - cur_;
-    keys_[nxt].reserve(std::max<uint64_t>(off, 1), stream_);
-    if (!k64_)
-        cnts_[nxt].reserve(std::max<uint64_t>(off, 1), stream_);
-    cuda_check(cudaMemcpyAsync(cursor_.p, h_cursor_.data(), n_inst * sizeof(unsigned long long),
-                               cudaMemcpyHostToDevice, stream_),
-               "upload cursors");
-    tot_.h2d_bytes += n_inst * sizeof(unsigned long long);
-    CompactArgs c;
-    c.table = table_.p;
-    c.cap = cap;
-    c.cursor = cursor_.p;
-    c.out_recs = keys_[nxt].p;
-    c.out_cnts = cnts_[nxt].p;
-    c.results = results_.p;
-    c.final_states = final_states_.p;
-    c.inst_off = inst_off_;
-    c.inst_mask = inst_mask_;
-    const int cgrid = (int)std::min<uint64_t>((cap + 255) / 256, (uint64_t)sms_ * 8);
-    cuda_check(cudaEventRecord(ev_[2], stream_), "cudaEventRecord");
-    launch_compact(k64_, c, cgrid, stream_);
-    cuda_check(cudaGetLastError(), "k_compact launch");
-    cuda_check(cudaEventRecord(ev_[3], stream_), "cudaEventRecord");
-    tot_.compact_launches++;
+    // Paused instances: their states move unchanged to the next frontier.
+    std::vector<std::pair<uint32_t, uint64_t>> moved;   // (id, new begin)
+    if (!paused.empty()) {
+        uint64_t need = off;
+        for (uint32_t id : paused)
+            need += inst_[id].seg_len;
+        keys_[nxt].reserve(std::max<uint64_t>(need, 1), stream_, off);
+        if (!k64_)
+            cnts_[nxt].reserve(std::max<uint64_t>(need, 1), stream_, off);
+        for (uint32_t id : paused) {
+            const Inst &in = inst_[id];
+            if (in.seg_len) {
+                cuda_check(cudaMemcpyAsync(keys_[nxt].p + off, keys_[cur_].p + in.seg_begin,
+                                           in.seg_len * sizeof(ulonglong2),
+                                           cudaMemcpyDeviceToDevice, stream_),
+                           "carry paused states");
+                if (!k64_)
+                    cuda_check(cudaMemcpyAsync(cnts_[nxt].p + off, cnts_[cur_].p + in.seg_begin,
+                                               in.seg_len * sizeof(unsigned long long),
+                                               cudaMemcpyDeviceToDevice, stream_),
+                               "carry paused states");
+            }
+            moved.push_back({id, off});
+            off += in.seg_len;
+        }
+    }
     if (opts_.keep_levels) {
         ulonglong2 *k = nullptr;
         unsigned long long *cn = nullptr;
@@ -609,10 +915,7 @@ StepStats Engine::step() {
         lvl_n_.push_back(off);
     }
     cuda_check(cudaEventRecord(ev_run_[1], stream_), "cudaEventRecord");
-    cuda_check(cudaStreamSynchronize(stream_), "k_compact");
-    float cms = 0.f;
-    cudaEventElapsedTime(&cms, ev_[2], ev_[3]);
-    st.compact_ms = cms;
+    cuda_check(cudaStreamSynchronize(stream_), "row end");
     float rms = 0.f;
     cudaEventElapsedTime(&rms, ev_run_[0], ev_run_[1]);
     tot_.run_ms = rms;
@@ -620,12 +923,25 @@ StepStats Engine::step() {
     // Advance the instances.
     std::vector<uint32_t> still;
     still.reserve(active_.size());
+    std::vector<uint32_t> keep_now, to_trace, ended;
     for (const auto &[id, begin] : nseg) {
         Inst &in = inst_[id];
         in.seg_begin = begin;
         in.seg_len = h_unique_[id];
         in.level_sizes.push_back(in.seg_len);
         in.row++;
+        if (in.mode == Mode::SolveOne) {
+            if (in.seg_len == 0) {
+                ended.push_back(id);
+            } else {
+                keep_now.push_back(id);
+                if (in.row == in.height)
+                    to_trace.push_back(id);
+                else
+                    still.push_back(id);
+            }
+            continue;
+        }
         if (in.row == in.height || in.seg_len == 0) {
             in.active = false;
             in.done = true;
@@ -668,11 +984,25 @@ StepStats Engine::step() {
         n_active_--;
         unfetched_.push_back(id);
     }
+    for (const auto &[id, begin] : moved) {
+        inst_[id].seg_begin = begin;
+        still.push_back(id);
+    }
     active_.swap(still);
     n_cur_ = off;
     cur_ = nxt;
+    // Solve-one: keep the new levels, trace the instances that completed
+    // their last row, and retry exhausted sampled attempts wider.
+    keep_levels_of(keep_now);
+    trace_solutions(to_trace);
+    for (uint32_t id : ended) {
+        if (inst_[id].sampled)
+            restart(id);
+        else
+            finish_solve_one(id, false);
+    }
     if (st.n_in)
-        growth_ = std::clamp((double)st.n_out / (double)st.n_in * 1.25, 1.0, 64.0);
+        growth_ = std::clamp((double)st.n_out / (double)st.n_in * 1.25, 1.0, 256.0);
 
     tot_.steps++;
     tot_.states_in += st.n_in;
@@ -681,7 +1011,206 @@ StepStats Engine::step() {
     tot_.expand_ms += st.expand_ms;
     tot_.compact_ms += st.compact_ms;
     tot_.peak_frontier = std::max<uint64_t>(tot_.peak_frontier, st.n_out);
+    tot_.paused += st.paused;
     return st;
+}
+
+void Engine::keep_levels_of(const std::vector<uint32_t> &ids) {
+    // One pool block per call for the current segments of `ids`, filled by
+    // one range-copy launch.
+    uint64_t total = 0;
+    for (uint32_t id : ids)
+        total += inst_[id].seg_len;
+    if (ids.empty() || total == 0)
+        return;
+    if (!pool_) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = opts_.device;
+        cuda_check(cudaMemPoolCreate(&pool_, &props), "cudaMemPoolCreate");
+        uint64_t keep_all = ~0ull;
+        cuda_check(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep_all),
+                   "cudaMemPoolSetAttribute");
+    }
+    LvlChunk ch;
+    cuda_check(cudaMallocFromPoolAsync(reinterpret_cast<void **>(&ch.keys),
+                                       total * sizeof(ulonglong2), pool_, stream_),
+               "cudaMallocFromPoolAsync");
+    ch.bytes = total * sizeof(ulonglong2);
+    if (!k64_) {
+        cuda_check(cudaMallocFromPoolAsync(reinterpret_cast<void **>(&ch.cnts),
+                                           total * sizeof(unsigned long long), pool_, stream_),
+                   "cudaMallocFromPoolAsync");
+        ch.bytes += total * sizeof(unsigned long long);
+    }
+    uint32_t ci;
+    if (!free_chunks_.empty()) {
+        ci = free_chunks_.back();
+        free_chunks_.pop_back();
+    } else {
+        ci = (uint32_t)chunks_.size();
+        chunks_.emplace_back();
+    }
+    std::vector<CopyRange> rg;
+    rg.reserve(ids.size());
+    uint64_t dst = 0;
+    for (uint32_t id : ids) {
+        Inst &in = inst_[id];
+        if (!in.seg_len)
+            continue;
+        rg.push_back({in.seg_begin, dst, in.seg_len});
+        in.levels.push_back({ci, dst, in.seg_len});
+        ch.refs++;
+        dst += in.seg_len;
+    }
+    chunks_[ci] = ch;
+    lvl_bytes_ += ch.bytes;
+    ranges_.reserve(rg.size(), stream_);
+    cuda_check(cudaMemcpyAsync(ranges_.p, rg.data(), rg.size() * sizeof(CopyRange),
+                               cudaMemcpyHostToDevice, stream_),
+               "upload ranges");
+    tot_.h2d_bytes += rg.size() * sizeof(CopyRange);
+    const int grid = (int)std::min<uint64_t>((rg.size() + 7) / 8, (uint64_t)sms_ * 8);
+    launch_copy_ranges(keys_[cur_].p, k64_ ? nullptr : cnts_[cur_].p, ch.keys, ch.cnts, ranges_.p,
+                       (uint32_t)rg.size(), grid, stream_);
+    cuda_check(cudaGetLastError(), "k_copy_ranges launch");
+    tot_.other_launches++;
+    // rg is pageable: the upload must have read it before it goes away.
+    cuda_check(cudaStreamSynchronize(stream_), "keep levels");
+}
+
+void Engine::drop_levels(Inst &in) {
+    for (const LevelRef &l : in.levels) {
+        LvlChunk &c = chunks_[l.chunk];
+        if (--c.refs == 0) {
+            if (c.keys)
+                cudaFreeAsync(c.keys, stream_);
+            if (c.cnts)
+                cudaFreeAsync(c.cnts, stream_);
+            lvl_bytes_ -= c.bytes;
+            c = LvlChunk{};
+            free_chunks_.push_back(l.chunk);
+        }
+    }
+    in.levels.clear();
+}
+
+void Engine::finish_solve_one(uint32_t id, bool found) {
+    Inst &in = inst_[id];
+    in.found = found;
+    in.result = found ? 1 : 0;
+    in.result_ready = true;
+    in.active = false;
+    in.done = true;
+    in.seg_len = 0;
+    drop_levels(in);
+    n_active_--;
+}
+
+void Engine::restart(uint32_t id) {
+    // The sampled attempt ended without a tiling: start again from the
+    // root with a 16x wider sample (exact from 2^24 states on).
+    Inst &in = inst_[id];
+    drop_levels(in);
+    in.row = 0;
+    in.seg_len = 0;
+    in.level_sizes.clear();
+    in.sampled = false;
+    in.growth = 256.0;
+    in.beam = in.beam >= (1ull << 20) ? 0 : in.beam * 16;
+    in.active = false;
+    n_active_--;
+    pending_.push_back(id);
+    tot_.restarts++;
+}
+
+void Engine::trace_solutions(const std::vector<uint32_t> &ids) {
+    if (ids.empty())
+        return;
+    std::vector<TraceJob> jobs;
+    std::vector<LevelPtr> lp;
+    for (uint32_t id : ids) {
+        const Inst &in = inst_[id];
+        if (in.levels.size() != (size_t)in.height + 1)
+            throw Error(kErrState, "solve-one level store incomplete");
+        TraceJob j{};
+        j.inst = id;
+        j.height = in.height;
+        j.lvl = (uint32_t)lp.size();
+        j.tag = seg_for(id, 0).tag;
+        jobs.push_back(j);
+        for (const LevelRef &l : in.levels) {
+            const LvlChunk &c = chunks_[l.chunk];
+            lp.push_back({c.keys + l.first, c.cnts ? c.cnts + l.first : nullptr, l.len});
+        }
+    }
+    jobs_.reserve(jobs.size(), stream_);
+    lvlptr_.reserve(lp.size(), stream_);
+    trace_out_.reserve(jobs.size(), stream_);
+    cuda_check(cudaMemcpyAsync(jobs_.p, jobs.data(), jobs.size() * sizeof(TraceJob),
+                               cudaMemcpyHostToDevice, stream_),
+               "upload trace jobs");
+    cuda_check(cudaMemcpyAsync(lvlptr_.p, lp.data(), lp.size() * sizeof(LevelPtr),
+                               cudaMemcpyHostToDevice, stream_),
+               "upload level pointers");
+    tot_.h2d_bytes += jobs.size() * sizeof(TraceJob) + lp.size() * sizeof(LevelPtr);
+    const int grid = (int)std::min<uint64_t>((jobs.size() + 7) / 8, (uint64_t)sms_ * 8);
+    launch_trace(k64_, insts_.p, plc_.p, lvlptr_.p, jobs_.p, (uint32_t)jobs.size(), trace_out_.p,
+                 grid, stream_);
+    cuda_check(cudaGetLastError(), "k_trace launch");
+    tot_.other_launches++;
+    std::vector<TraceOut> out(jobs.size());
+    cuda_check(cudaMemcpyAsync(out.data(), trace_out_.p, out.size() * sizeof(TraceOut),
+                               cudaMemcpyDeviceToHost, stream_),
+               "read trace");
+    cuda_check(cudaStreamSynchronize(stream_), "k_trace");
+    tot_.d2h_bytes += out.size() * sizeof(TraceOut);
+    for (size_t k = 0; k < ids.size(); k++) {
+        const uint32_t id = ids[k];
+        Inst &in = inst_[id];
+        const TraceOut &o = out[k];
+        if (o.status != 0) {
+            in.active = true;   // fail_instance retires an active instance
+            fail_instance(id, kErrState,
+                          o.status == 1 ? "solve-one trace: witness without parent"
+                                        : "solve-one trace: no fill between kept states");
+            continue;
+        }
+        const uint32_t W = in.width, H = in.height, cells = W * H;
+        in.tgrid.assign(cells, -1);
+        in.sgrid.assign(cells, -1);
+        int step = 0;
+        for (uint32_t r = 0; r < H; r++)
+            for (uint32_t q = 0; q < o.nfill[r]; q++, step++) {
+                const uint32_t pi = o.plc[r][q];
+                for (uint64_t bits = in.lib.plc[pi].mask; bits; bits &= bits - 1) {
+                    const uint32_t cell = r * W + (uint32_t)__builtin_ctzll(bits);
+                    if (cell < cells) {
+                        in.tgrid[cell] = (int8_t)in.lib.plc_type[pi];
+                        in.sgrid[cell] = (int16_t)step;
+                    }
+                }
+            }
+        finish_solve_one(id, true);
+    }
+}
+
+bool Engine::solution(uint32_t id, int8_t *type_grid, int16_t *step_grid) {
+    const Inst &in = inst_.at(id);
+    if (in.mode != Mode::SolveOne)
+        throw Error(kErrState, "not a solve-one instance");
+    if (!in.done)
+        throw Error(kErrState, "instance has not finished");
+    if (in.status)
+        throw Error(in.status, in.error);
+    if (!in.found)
+        return false;
+    if (type_grid)
+        std::memcpy(type_grid, in.tgrid.data(), in.tgrid.size());
+    if (step_grid)
+        std::memcpy(step_grid, in.sgrid.data(), in.sgrid.size() * sizeof(int16_t));
+    return true;
 }
 
 uint64_t Engine::bucket_count(uint32_t id, uint32_t pattern) {
@@ -733,6 +1262,8 @@ uint64_t Engine::count(uint32_t id) {
     Inst &in = inst_.at(id);
     if (!in.done)
         throw Error(kErrState, "instance has not finished");
+    if (in.status)
+        throw Error(in.status, in.error);
     if (!in.result_ready)
         sync_results();
     return in.result;

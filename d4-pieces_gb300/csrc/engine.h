@@ -20,6 +20,7 @@
 
 #include "d4e_types.h"
 #include "geometry.h"
+#include "kernels.h"
 
 namespace d4e {
 
@@ -67,7 +68,19 @@ struct EngineOpts {
     uint64_t chunk_states = 1024;  // largest number of work items a warp takes at once
     uint64_t max_frontier = 0;     // abort when a row yields more states (0 = no limit)
     KeyMode key_mode = KeyMode::Auto;  // Auto: K64 when every instance's packed key fits
+    // Device bytes the frontiers and the hash table may hold together
+    // (0 = the whole device less 10%).
+    uint64_t memory_budget = 0;
+    // A failing instance (its frontier limit, or a row that cannot fit the
+    // device alone) ends with an error status instead of failing step().
+    bool isolate_failures = false;
+    // K64 layout fixed at construction with this many instance-id bits
+    // (0 = layout chosen from the instances, see fix_key_mode).  Instances
+    // whose window + counter bits exceed 63 - k64_inst_bits are rejected.
+    uint32_t k64_inst_bits = 0;
 };
+
+enum class Mode : uint32_t { Count = 0, SolveOne = 1 };
 
 struct InstanceSpec {
     uint32_t width = 8;
@@ -77,12 +90,18 @@ struct InstanceSpec {
     const uint32_t *counts = nullptr;
     uint32_t n_pieces = 0;
     uint32_t sym = 0xFFu;
+    Mode mode = Mode::Count;
+    uint64_t max_states = 0;             // per-row frontier limit (0 = none)
+    uint64_t beam = 0;                   // solve-one: first sampled-frontier width (0 = exact)
 };
 
 struct StepStats {
     uint64_t n_in = 0, n_raw = 0, n_out = 0;
     float expand_ms = 0.f, compact_ms = 0.f;
     uint32_t retries = 0;
+    uint32_t paused = 0;          // instances that waited for memory this row
+    uint32_t groups = 0;          // k_expand groups (after splits)
+    uint32_t failed = 0;          // instances that ended with an error this row
     uint64_t table_cap = 0;
 };
 
@@ -91,9 +110,18 @@ struct Totals {
     uint64_t states_in = 0, states_raw = 0, states_out = 0;
     double expand_ms = 0.0, compact_ms = 0.0;
     uint64_t expand_launches = 0, compact_launches = 0, other_launches = 0, retries = 0;
+    uint64_t paused = 0, splits = 0, failed = 0, restarts = 0;
     uint64_t peak_frontier = 0;
     uint64_t h2d_bytes = 0, d2h_bytes = 0;
     double run_ms = 0.0;           // CUDA-event time from the first step to the last
+};
+
+// One kept frontier level of a solve-one instance: `len` records from
+// `first` on in level chunk `chunk` (a device block shared by the instances
+// kept in the same step).
+struct LevelRef {
+    uint32_t chunk;
+    uint64_t first, len;
 };
 
 class Engine {
@@ -117,8 +145,20 @@ public:
     bool done(uint32_t id) const { return inst_.at(id).done; }
     uint32_t row(uint32_t id) const { return inst_.at(id).row; }
     uint32_t height(uint32_t id) const { return inst_.at(id).height; }
+    uint32_t width(uint32_t id) const { return inst_.at(id).width; }
+    // Device bytes (frontier records + table slots) the instance's next row
+    // is expected to need, and the most any of its rows needed so far.
+    uint64_t projected_bytes(uint32_t id) const;
+    uint64_t peak_bytes(uint32_t id) const;
     uint64_t frontier_size(uint32_t id) const { return inst_.at(id).seg_len; }
     uint64_t count(uint32_t id);                        // tilings (valid once done)
+    int status(uint32_t id) const { return inst_.at(id).status; }   // 0 or an ErrCode
+    const std::string &error(uint32_t id) const { return inst_.at(id).error; }
+    // Solve-one result: true and the tiling (row-major type grid, step grid,
+    // width * height cells each, -1 = not covered) when one exists.
+    bool solution(uint32_t id, int8_t *type_grid, int16_t *step_grid);
+    // Frees a finished instance's id for reuse by a later add().
+    void release(uint32_t id);
     const std::vector<uint64_t> &level_sizes(uint32_t id) const { return inst_.at(id).level_sizes; }
     uint64_t next_size_estimate(uint32_t id) const;
     // States of the instance's frontier whose current row equals `pattern`.
@@ -149,9 +189,31 @@ private:
         uint64_t result = 0;
         std::vector<uint64_t> level_sizes;
         unsigned long long root_window = 0;
+        double growth = 256.0;       // expected children per state on the next row
+        Mode mode = Mode::Count;
+        uint64_t limit = 0;          // per-row frontier limit (0 = none)
+        int status = 0;              // 0 or the ErrCode it failed with
+        std::string error;
+        // Solve-one: sampled-frontier width of the current attempt (0 =
+        // exact), whether a row was sampled, and the kept levels.
+        uint64_t beam = 0;
+        bool sampled = false;
+        std::vector<LevelRef> levels;
+        bool found = false;
+        std::vector<int8_t> tgrid;
+        std::vector<int16_t> sgrid;
     };
 
     void ensure_inst_capacity(size_t n);
+    void fail_instance(uint32_t id, int code, const std::string &msg);
+    // Solve-one support: kept levels, tracing, restarts with a wider sample.
+    void keep_levels_of(const std::vector<uint32_t> &ids);
+    void drop_levels(Inst &in);
+    void trace_solutions(const std::vector<uint32_t> &ids);
+    void finish_solve_one(uint32_t id, bool found);
+    void restart(uint32_t id);
+    uint64_t frontier_bytes(int buf) const;
+    double memory_limit(double device_avail) const;
     void fix_key_mode();
     void flush_uploads();
     int expand_occupancy();
@@ -178,6 +240,7 @@ private:
     std::vector<uint32_t> pending_upload_;   // descriptors/tables not yet on the device
     std::vector<uint32_t> active_;           // instances with a frontier segment
     std::vector<uint32_t> unfetched_;        // finished, result still on the device
+    std::vector<uint32_t> free_ids_;         // released ids, reused by add()
     uint32_t n_active_ = 0;
 
     DevBuf<Plc> plc_;
@@ -208,9 +271,29 @@ private:
     std::vector<unsigned long long *> lvl_cnts_;
     std::vector<uint64_t> lvl_n_;
 
+    // Kept levels of solve-one instances: one block per step from a stream-
+    // ordered pool, freed when no instance refers to it any more.
+    struct LvlChunk {
+        ulonglong2 *keys = nullptr;
+        unsigned long long *cnts = nullptr;
+        uint64_t bytes = 0;
+        uint32_t refs = 0;
+    };
+    std::vector<LvlChunk> chunks_;
+    std::vector<uint32_t> free_chunks_;
+    uint64_t lvl_bytes_ = 0;
+    cudaMemPool_t pool_ = nullptr;
+    DevBuf<CopyRange> ranges_;
+    DevBuf<unsigned long long> keep_max_;
+    std::vector<unsigned long long> h_keep_max_;
+    DevBuf<TraceJob> jobs_;
+    DevBuf<LevelPtr> lvlptr_;
+    DevBuf<TraceOut> trace_out_;
+
     Totals tot_;
     bool run_started_ = false;
     std::vector<unsigned int> h_unique_;
+    std::vector<unsigned int> h_grp_unique_;   // one group's read-back
     std::vector<unsigned long long> h_cursor_;
 };
 

@@ -18,6 +18,8 @@
 
 #include <cuda_runtime.h>
 
+#include "state_hash.cuh"
+
 namespace d4e {
 
 namespace {
@@ -25,14 +27,6 @@ namespace {
 constexpr int kExpandBlock = 256;
 constexpr int kCompactBlock = 256;
 
-__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
-    x ^= x >> 33;
-    x *= 0xff51afd7ed558ccdull;
-    x ^= x >> 33;
-    x *= 0xc4ceb9fe1a85ec53ull;
-    x ^= x >> 33;
-    return x;
-}
 
 // Home slot in a table of `cap` slots (any capacity): the high half of
 // hash * cap maps the 64-bit hash uniformly onto [0, cap).
@@ -66,9 +60,20 @@ __device__ __forceinline__ void cas128(unsigned long long *addr,
 
 // Insert with multiplicity cnt (linear probing).  Returns 1 for a newly
 // claimed key, 0 for an existing one, -1 when the probe limit was reached.
+// The value field of a slot: counts are summed; witnesses (solve-one
+// instances) keep the largest.
+__device__ __forceinline__ void merge_value(unsigned long long *v, unsigned long long x, bool wmax) {
+    if (wmax)
+        atomicMax(v, x);
+    else
+        atomicAdd(v, x);
+}
+
+// Insert with multiplicity cnt (linear probing).  Returns 1 for a newly
+// claimed key, 0 for an existing one, -1 when the probe limit was reached.
 __device__ __forceinline__ int insert64(Slot16 *__restrict__ T, unsigned long long cap,
                                         unsigned long long key, unsigned long long cnt,
-                                        unsigned int max_probe) {
+                                        unsigned int max_probe, bool wmax = false) {
     unsigned long long h = home64(key, cap);
     for (unsigned int p = 0; p < max_probe; ++p) {
         // A naturally aligned 8-byte load is single-copy atomic: a key seen
@@ -77,12 +82,12 @@ __device__ __forceinline__ int insert64(Slot16 *__restrict__ T, unsigned long lo
         if (k == 0ull) {
             k = atomicCAS(&T[h].key, 0ull, key);
             if (k == 0ull) {
-                atomicAdd(&T[h].cnt, cnt);
+                merge_value(&T[h].cnt, cnt, wmax);
                 return 1;
             }
         }
         if (k == key) {
-            atomicAdd(&T[h].cnt, cnt);
+            merge_value(&T[h].cnt, cnt, wmax);
             return 0;
         }
         h = next_slot(h, cap);
@@ -92,20 +97,23 @@ __device__ __forceinline__ int insert64(Slot16 *__restrict__ T, unsigned long lo
 
 __device__ __forceinline__ int insert128(Slot32 *__restrict__ T, unsigned long long cap,
                                          unsigned long long k0, unsigned long long k1,
-                                         unsigned long long cnt, unsigned int max_probe) {
+                                         unsigned long long cnt, unsigned int max_probe,
+                                         bool wmax = false) {
     unsigned long long h = home128(k0, k1, cap);
     for (unsigned int p = 0; p < max_probe; ++p) {
         unsigned long long o0, o1;
         cas128(&T[h].k0, 0ull, 0ull, k0, k1, o0, o1);
         const bool claimed = (o0 | o1) == 0ull;
         if (claimed || (o0 == k0 && o1 == k1)) {
-            atomicAdd(&T[h].cnt, cnt);
+            merge_value(&T[h].cnt, cnt, wmax);
             return claimed ? 1 : 0;
         }
         h = next_slot(h, cap);
     }
     return -1;
 }
+
+
 
 // Membership lookups (the table is read-only while they run).
 __device__ __forceinline__ bool find64(const Slot16 *__restrict__ T, unsigned long long cap,
@@ -288,12 +296,15 @@ __device__ __forceinline__ void flush_children(const ExpandArgs &a, const WarpSt
     uint32_t inst = 0xFFFFFFFFu;
     if ((int)lane < n) {
         const int j = base + (int)lane;
-        inst = ws.inst[j];
+        const uint32_t si = ws.inst[j];
+        const bool wmax = (si >> 31) != 0u;   // solve-one instance: value = witness
+        inst = si & 0x7FFFFFFFu;
         if constexpr (K64)
-            r = insert64(static_cast<Slot16 *>(a.table), a.cap, ws.k0[j], ws.cnt[j], a.max_probe);
+            r = insert64(static_cast<Slot16 *>(a.table), a.cap, ws.k0[j], ws.cnt[j], a.max_probe,
+                         wmax);
         else
             r = insert128(static_cast<Slot32 *>(a.table), a.cap, ws.k0[j], ws.k1[j], ws.cnt[j],
-                          a.max_probe);
+                          a.max_probe, wmax);
     }
     if (__any_sync(0xffffffffu, r < 0) && lane == 0)
         atomicOr(a.status, kStatusTableOverflow);
@@ -339,6 +350,7 @@ k_expand(ExpandArgs a) {
     uint32_t W = 0, rowmask = 0, dyn_bits = 0;
     unsigned long long usedmask = 0, dynmask = 0;
     unsigned long long w = 0, u = 0, cnt = 0, sidx = 0;
+    bool wit = false;   // solve-one instance: cnt holds the parent's witness
     uint32_t scol = 0, depth = 0, idx = 0, min_depth = 0;
     unsigned long long rw = 0, ru = 0;   // walk state at the root of the lane's subtree
     int nbuf = 0;   // warp-uniform: staged children
@@ -389,14 +401,15 @@ k_expand(ExpandArgs a) {
                 usedmask = (1ull << d->used_bits) - 1ull;
                 const unsigned long long si = item / fan;
                 const ulonglong2 rec = a.recs[si];
+                wit = (d->flags & kInstWitness) != 0u;
                 if constexpr (K64) {
                     w = (rec.x & dynmask) | sg->hi_board;
                     u = (rec.x >> dyn_bits) & usedmask;
-                    cnt = rec.y;
+                    cnt = wit ? witness64(rec.x, sg->tag) : rec.y;
                 } else {
                     w = rec.x;
                     u = rec.y & kUsedMask128;
-                    cnt = a.cnts[si];
+                    cnt = wit ? witness128(rec.x, rec.y) : a.cnts[si];
                 }
                 sidx = 0;
                 scol = 0;
@@ -471,6 +484,7 @@ k_expand(ExpandArgs a) {
                 if (recv) {
                     sg = reinterpret_cast<const Seg *>(d_sg);
                     d = a.insts + sg->inst;
+                    wit = (d->flags & kInstWitness) != 0u;
                     plc = a.plc + d->plc_off;
                     W = d->width;
                     rowmask = (1u << W) - 1u;
@@ -580,7 +594,7 @@ k_expand(ExpandArgs a) {
             ws.k0[pos] = ck0;
             ws.k1[pos] = ck1;
             ws.cnt[pos] = cnt;
-            ws.inst[pos] = sg->inst;
+            ws.inst[pos] = sg->inst | (wit ? 0x80000000u : 0u);
             ++raw;
         }
         nbuf += __popc(em);
@@ -635,7 +649,20 @@ k_compact(CompactArgs a) {
         }
         const unsigned long long cur = occ ? a.cursor[inst] : 0ull;
         const bool fin = occ && cur == kCursorFinal;
-        const bool store = occ && !fin;
+        bool store = occ && !fin && cur != kCursorDrop;
+        if (store && a.keep_max) {
+            // Sampled frontier: keep the states whose instance-free hash is
+            // below the instance's threshold.
+            const unsigned long long km = a.keep_max[inst];
+            if (km != ~0ull) {
+                unsigned long long wid;
+                if constexpr (K64)
+                    wid = k0 & ((1ull << a.inst_off) - 1ull);
+                else
+                    wid = witness128(k0, k1);
+                store = sample_hash(wid) <= km;
+            }
+        }
         // Warp-aggregated cursor bump per instance.
         const unsigned peers = __match_any_sync(0xffffffffu, store ? inst : 0xFFFFFFFFu);
         if (store) {

@@ -43,6 +43,9 @@ struct CompactArgs {
     unsigned int *final_states;      // per instance: number of final states
     uint32_t inst_off;               // K64: position of the instance id in a key
     unsigned long long inst_mask;    // K64: instance id mask (after shifting)
+    // Per instance: keep a state only if its sample hash is <= keep_max
+    // (~0 = keep all).  nullptr = no sampling.
+    const unsigned long long *keep_max;
 };
 
 // Resident k_expand blocks per SM (for sizing its persistent grid).
@@ -99,5 +102,48 @@ void launch_select(const ulonglong2 *recs, const unsigned char *alive, unsigned 
 void launch_count_pattern(const ulonglong2 *recs, unsigned long long n, unsigned long long mask,
                           unsigned long long value, unsigned long long *out, int grid,
                           cudaStream_t s);
+
+}  // namespace d4e
+
+namespace d4e {
+
+// Solve-one ----------------------------------------------------------------
+// A kept level of one solve-one instance.
+struct LevelPtr {
+    const ulonglong2 *recs;          // K64 {key, witness} records / K128 keys
+    const unsigned long long *cnts;  // K128 witnesses
+    unsigned long long len;
+};
+
+struct TraceJob {
+    uint32_t inst;
+    uint32_t height;
+    uint32_t lvl;                    // first of height + 1 LevelPtr entries (level 0 = root)
+    uint32_t pad;
+    unsigned long long tag;          // the instance's key tag
+};
+
+struct TraceOut {
+    uint32_t status;                 // 0 = traced; 1 = a witness had no parent; 2 = no fill
+    uint8_t nfill[kMaxHeight];       // placements completing each row
+    uint16_t plc[kMaxHeight][kMaxWidth];   // instance-relative placement indices
+};
+
+// For every job: pick the final state with the largest identity, follow the
+// parent witnesses back to the root (largest identity among matching
+// parents), then find each row's first fill (depth-first order) leading
+// from the chosen parent to the chosen child.  One warp per job.
+void launch_trace(bool k64, const InstDesc *insts, const Plc *plc, const LevelPtr *levels,
+                  const TraceJob *jobs, uint32_t n_jobs, TraceOut *out, int grid,
+                  cudaStream_t s);
+
+// Copies record ranges (and K128 counts when cnts are given) between
+// frontier buffers: one warp per range.
+struct CopyRange {
+    unsigned long long src, dst, len;
+};
+void launch_copy_ranges(const ulonglong2 *src, const unsigned long long *src_cnts, ulonglong2 *dst,
+                        unsigned long long *dst_cnts, const CopyRange *ranges, uint32_t n,
+                        int grid, cudaStream_t s);
 
 }  // namespace d4e

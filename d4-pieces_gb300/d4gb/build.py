@@ -75,7 +75,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     OBJ_DIR.mkdir(exist_ok=True)
     LIB_DIR.mkdir(exist_ok=True)
     srcs = _sources()
-    headers = sorted(CSRC.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
+    headers = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
     if force:
         for o in OBJ_DIR.glob("*.o"):
             o.unlink()

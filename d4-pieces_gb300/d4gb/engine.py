@@ -23,6 +23,11 @@ if not LIB_PATH.exists():
 _lib = C.CDLL(str(LIB_PATH))
 
 D4E_OK = 0
+D4E_ERR_INVALID = -1
+D4E_ERR_CUDA = -2
+D4E_ERR_NOMEM = -3
+D4E_ERR_UNSUPPORTED = -4
+D4E_ERR_STATE = -5
 D4E_KEEP_LEVELS = 1
 D4E_BATCH_SEQUENTIAL = 1
 
@@ -56,6 +61,74 @@ class Stats(C.Structure):
         ("run_ms", C.c_double),
         ("record_bytes", C.c_uint64),
         ("slot_bytes", C.c_uint64),
+        ("paused", C.c_uint64),
+        ("splits", C.c_uint64),
+        ("failed", C.c_uint64),
+        ("restarts", C.c_uint64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class BatchOpts(C.Structure):
+    _fields_ = [
+        ("mode", C.c_uint32),
+        ("flags", C.c_uint32),
+        ("device", C.c_int32),
+        ("reserved", C.c_uint32),
+        ("memory_budget", C.c_uint64),
+        ("max_states", C.c_uint64),
+        ("beam", C.c_uint64),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("tag", C.c_uint64),
+        ("status", C.c_int32),
+        ("mode", C.c_uint32),
+        ("count", C.c_uint64),
+        ("found", C.c_uint32),
+        ("rows", C.c_uint32),
+        ("queued_ms", C.c_double),
+        ("latency_ms", C.c_double),
+        ("grid", C.c_int8 * 512),
+        ("steps", C.c_int16 * 512),
+    ]
+
+    def as_dict(self, width: int = 0, height: int = 0) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("grid", "steps")}
+        if self.found and width and height:
+            n = width * height
+            d["grid"] = np.frombuffer(bytes(self.grid), dtype=np.int8)[:n] \
+                .reshape(height, width).copy()
+            d["steps"] = np.frombuffer(bytes(self.steps), dtype=np.int16)[:n] \
+                .reshape(height, width).copy()
+        return d
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32),
+        ("max_active", C.c_uint32),
+        ("memory_budget", C.c_uint64),
+        ("max_states", C.c_uint64),
+        ("beam", C.c_uint64),
+    ]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_uint64),
+        ("admitted", C.c_uint64),
+        ("completed", C.c_uint64),
+        ("failed", C.c_uint64),
+        ("steps", C.c_uint64),
+        ("peak_active", C.c_uint64),
+        ("peak_projected", C.c_uint64),
+        ("states_out", C.c_uint64),
+        ("busy_ms", C.c_double),
     ]
 
     def as_dict(self) -> dict:
@@ -108,6 +181,14 @@ _sig("d4e_searcher_set_limit", C.c_int, C.c_void_p, C.c_uint64)
 _sig("d4e_searcher_destroy", None, C.c_void_p)
 _sig("d4e_batch_count", C.c_int, C.POINTER(Instance), C.c_uint32, C.c_uint32, C.c_int32, _u64p,
      C.POINTER(Stats))
+_sig("d4e_batch_run", C.c_int, C.POINTER(Instance), C.c_uint32, C.POINTER(BatchOpts),
+     C.POINTER(Result), C.POINTER(Stats))
+_sig("d4e_server_create", C.c_int, C.POINTER(ServerOpts), C.POINTER(C.c_void_p))
+_sig("d4e_server_submit", C.c_int, C.c_void_p, C.POINTER(Instance), C.c_uint32, C.c_uint64)
+_sig("d4e_server_poll", C.c_int, C.c_void_p, C.POINTER(Result), C.c_uint32, _u32p)
+_sig("d4e_server_drain", C.c_int, C.c_void_p, C.c_double)
+_sig("d4e_server_stats_get", C.c_int, C.c_void_p, C.POINTER(ServerStats))
+_sig("d4e_server_destroy", None, C.c_void_p)
 _sig("d4e_canonical_grid", C.c_int, C.c_uint32, C.c_uint32, _u8p, _i8p, _i8p)
 _sig("d4e_count_noalloc", C.c_int, C.POINTER(Instance), C.c_void_p, _u64p, _u64p)
 
@@ -288,6 +369,73 @@ def batch_count(problems, sequential: bool = False, device: int = 0):
     _check(_lib.d4e_batch_count(arr, len(problems), D4E_BATCH_SEQUENTIAL if sequential else 0,
                                 device, out, C.byref(st)))
     return list(out)[: len(problems)], st.as_dict()
+
+
+MODE_COUNT = 0
+MODE_SOLVE_ONE = 1
+
+
+D4E_BATCH_WIDE_KEYS = 2
+
+
+def batch_run(problems, mode: int = MODE_COUNT, sequential: bool = False, device: int = 0,
+              memory_budget: int = 0, max_states: int = 0, beam: int = 0,
+              wide_keys: bool = False):
+    """Runs a batch through d4e_batch_run; returns (results, stats dict).
+    Each result is a dict (status, count, found, rows, latency_ms, and for a
+    found solve-one tiling height x width "grid" (types) and "steps")."""
+    arr, keep = _instances(problems)
+    n = len(problems)
+    res = (Result * max(n, 1))()
+    flags = (D4E_BATCH_SEQUENTIAL if sequential else 0) | (D4E_BATCH_WIDE_KEYS if wide_keys else 0)
+    o = BatchOpts(mode, flags, device, 0, memory_budget, max_states, beam)
+    st = Stats()
+    _check(_lib.d4e_batch_run(arr, n, C.byref(o), res, C.byref(st)))
+    return ([res[i].as_dict(problems[i].width, problems[i].height) for i in range(n)],
+            st.as_dict())
+
+
+class Server:
+    """Continuous-batching request server (d4e_server_*)."""
+
+    def __init__(self, device: int = 0, memory_budget: int = 0, max_states: int = 0,
+                 beam: int = 0, max_active: int = 0):
+        o = ServerOpts(device, max_active, memory_budget, max_states, beam)
+        h = C.c_void_p()
+        _check(_lib.d4e_server_create(C.byref(o), C.byref(h)))
+        self._h = h
+        self._shape = {}
+
+    def submit(self, problem, mode: int, tag: int) -> None:
+        arr, keep = _instances([problem])
+        self._shape[tag] = (problem.width, problem.height)
+        _check(_lib.d4e_server_submit(self._h, arr, mode, tag))
+
+    def poll(self, max_results: int = 4096):
+        out = (Result * max_results)()
+        n = C.c_uint32()
+        _check(_lib.d4e_server_poll(self._h, out, max_results, C.byref(n)))
+        res = []
+        for i in range(n.value):
+            w, h = self._shape.pop(out[i].tag, (0, 0))
+            res.append(out[i].as_dict(w, h))
+        return res
+
+    def drain(self, timeout_s: float = 600.0) -> None:
+        _check(_lib.d4e_server_drain(self._h, timeout_s))
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(_lib.d4e_server_stats_get(self._h, C.byref(st)))
+        return st.as_dict()
+
+    def close(self) -> None:
+        if self._h:
+            _lib.d4e_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
 
 
 def count(problem, device: int = 0) -> int:

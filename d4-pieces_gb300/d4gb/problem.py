@@ -126,6 +126,38 @@ def merge_pieces(shapes: List[int]):
     return types, counts
 
 
+def verify_tiling(p: "Problem", type_grid, step_grid) -> bool:
+    """Independent cover check of a reported tiling: every board cell is
+    covered by exactly one placement and holes by none; each placement
+    (cells sharing a step number) is an allowed transform of its piece type;
+    no type is used more often than its count."""
+    H, W = p.height, p.width
+    used = [0] * len(p.shapes)
+    groups = {}
+    for r in range(H):
+        for c in range(W):
+            t = int(type_grid[r][c])
+            s = int(step_grid[r][c])
+            on_board = (p.rows[r] >> c) & 1
+            if not on_board:
+                if t != -1 or s != -1:
+                    return False
+                continue
+            if s < 0 or not 0 <= t < len(p.shapes):
+                return False
+            g = groups.setdefault(s, [t, []])
+            if g[0] != t:
+                return False
+            g[1].append((r, c))
+    for t, cells in groups.values():
+        shape = normalize(cells_to_shape(cells))
+        forms = {transform(p.shapes[t], k) for k in range(8) if (p.sym >> k) & 1}
+        if shape not in forms:
+            return False
+        used[t] += 1
+    return all(u <= n for u, n in zip(used, p.counts))
+
+
 # ---------------------------------------------------------------------------
 # Workloads
 # ---------------------------------------------------------------------------

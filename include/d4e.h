@@ -165,6 +165,10 @@ typedef struct d4e_stats {
     double run_ms;              /* CUDA-event time from the first row's start to the last row's end */
     uint64_t record_bytes;      /* bytes per frontier state: 16 (packed 64-bit keys) or 24 */
     uint64_t slot_bytes;        /* bytes per hash-table slot: 16 or 32 */
+    uint64_t paused;            /* instance-rows that waited for device memory */
+    uint64_t splits;            /* batch groups split after a table overflow */
+    uint64_t failed;            /* instances that ended with an error */
+    uint64_t restarts;          /* solve-one attempts redone with a wider sample */
 } d4e_stats;
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st);
@@ -193,6 +197,7 @@ typedef struct d4e_instance {
 } d4e_instance;
 
 #define D4E_BATCH_SEQUENTIAL 1u /* one puzzle at a time, one launch sequence per puzzle */
+#define D4E_BATCH_WIDE_KEYS 2u  /* d4e_batch_run: the general 128-bit key encoding for all */
 
 /* Counts the tilings of every instance.  Default: all instances advance
  * together, one k_expand + one k_compact launch per board row for the whole
@@ -200,6 +205,102 @@ typedef struct d4e_instance {
  * per-puzzle path).  counts[i] receives instance i's count.  st may be NULL. */
 int d4e_batch_count(const d4e_instance *insts, uint32_t n, uint32_t flags, int32_t device,
                     uint64_t *counts, d4e_stats *st);
+
+#define D4E_MODE_COUNT 0u      /* solve-all: count every tiling */
+#define D4E_MODE_SOLVE_ONE 1u  /* one tiling, or none when there is none */
+
+typedef struct d4e_batch_opts {
+    uint32_t mode;              /* D4E_MODE_* for every instance */
+    uint32_t flags;             /* D4E_BATCH_SEQUENTIAL */
+    int32_t device;
+    uint32_t reserved;
+    uint64_t memory_budget;     /* device bytes for frontiers + table (0 = device less 10%) */
+    uint64_t max_states;        /* per-instance limit on one row's frontier (0 = none) */
+    uint64_t beam;              /* solve-one: states kept per row on the first attempt
+                                   (0 = exact); see d4e_batch_run */
+} d4e_batch_opts;
+
+/* Result of one instance (batch) or request (server). */
+typedef struct d4e_result {
+    uint64_t tag;               /* batch: instance index; server: the submit tag */
+    int32_t status;             /* D4E_OK, or the error the instance ended with */
+    uint32_t mode;              /* D4E_MODE_* */
+    uint64_t count;             /* count mode: tilings; solve-one: 1 when found */
+    uint32_t found;             /* solve-one: grid holds a tiling */
+    uint32_t rows;              /* board rows completed */
+    double queued_ms;           /* server: submit -> admitted to the device */
+    double latency_ms;          /* submit (server) or batch start -> result */
+    int8_t grid[512];           /* solve-one: piece type per cell, row-major
+                                   (width * height cells), -1 = not covered */
+    int16_t steps[512];         /* solve-one: placement number per cell (anchor
+                                   order), -1 = not covered */
+} d4e_result;
+
+/* Runs a batch.  Instances advance together, one k_expand + k_compact pair
+ * per board row for the whole batch (grouped when memory runs short;
+ * instances that do not fit wait, in order, until memory frees up).  With
+ * D4E_BATCH_SEQUENTIAL each instance runs alone instead.  A failing
+ * instance (its max_states, or a row the device cannot hold) gets an error
+ * status; the others are unaffected.
+ *
+ * Solve-one: every row is de-duplicated as in counting; with beam > 0 a row
+ * whose distinct states exceed beam keeps about beam of them, chosen by a
+ * hash of the state alone.  When such an attempt dies out it is redone with
+ * a 16x wider sample, and exactly from 2^24 states on, so "not found" is
+ * always exact.  The tiling reported is the same whether the instance runs
+ * alone or in any batch.  results[i].tag = i. */
+int d4e_batch_run(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
+                  d4e_result *results, d4e_stats *st);
+
+/* ------------------------------------------------------------------------
+ * Serving: a request loop on a native worker thread.  No counterpart in the
+ * reference (its SearcherFactory runs a fixed job list).
+ *
+ * Requests queue on submit and are admitted in arrival order while the
+ * projected device bytes of the admitted requests (frontier + hash table of
+ * their next row) stay within memory_budget; admitted requests join the
+ * running batch at its next row, so work of requests that arrived at
+ * different times shares each k_expand / k_compact launch.  Results are the
+ * same as alone (counts exact; solve-one tilings as in d4e_batch_run).
+ * ---------------------------------------------------------------------- */
+typedef struct d4e_server d4e_server;
+
+typedef struct d4e_server_opts {
+    int32_t device;
+    uint32_t max_active;        /* requests on the device at once (0 = 8192) */
+    uint64_t memory_budget;     /* admission budget in bytes (0 = 150 GB, capped at the
+                                   device's memory less 10%) */
+    uint64_t max_states;        /* per-request limit on one row's frontier (0 = none) */
+    uint64_t beam;              /* solve-one first sample width (0 = exact) */
+} d4e_server_opts;
+
+int d4e_server_create(const d4e_server_opts *opts, d4e_server **out);
+
+/* Queues a request (the instance is copied).  Thread-safe. */
+int d4e_server_submit(d4e_server *s, const d4e_instance *inst, uint32_t mode, uint64_t tag);
+
+/* Moves up to max finished results into out; *n receives the number.
+ * Thread-safe. */
+int d4e_server_poll(d4e_server *s, d4e_result *out, uint32_t max, uint32_t *n);
+
+/* Waits until every submitted request has a result (or timeout_s passes:
+ * D4E_ERR_STATE). */
+int d4e_server_drain(d4e_server *s, double timeout_s);
+
+typedef struct d4e_server_stats {
+    uint64_t submitted, admitted, completed, failed;
+    uint64_t steps;             /* batch rows run */
+    uint64_t peak_active;       /* most requests on the device at once */
+    uint64_t peak_projected;    /* largest projected bytes admitted */
+    uint64_t states_out;        /* distinct states produced (all requests) */
+    double busy_ms;             /* worker time spent in device steps */
+} d4e_server_stats;
+
+int d4e_server_stats_get(d4e_server *s, d4e_server_stats *st);
+
+/* Stops the worker (requests still queued are dropped) and frees the device
+ * memory. */
+void d4e_server_destroy(d4e_server *s);
 
 /* ------------------------------------------------------------------------
  * Counting without device allocation.  No counterpart in the reference.
