@@ -47,7 +47,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--seed", type=int, default=SINGLE_LARGE_SEED)
-    ap.add_argument("--workload", choices=("single_large", "medium", "batched", "batched_one"),
+    ap.add_argument("--workload", choices=("single_large", "medium", "batched", "batched_one",
+                                           "serve"),
                     default="single_large",
                     help="medium = 8x10 board, 78 cells, 16 pieces (profiling case: frontier "
                          "of ~18M states, a few hundred MB -- larger than L2, a few GB at most)")
@@ -55,8 +56,14 @@ def parse_args():
                     help="batched workload: number of mix instances (seeded)")
     ap.add_argument("--max-states", type=int, default=20_000_000,
                     help="batched workloads: per-instance limit on one row's frontier")
-    ap.add_argument("--beam", type=int, default=256,
+    ap.add_argument("--beam", type=int, default=1024,
                     help="batched solve-one: first sampled-frontier width")
+    ap.add_argument("--rate", type=float, default=2000.0, help="serve: arrivals per second")
+    ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
+    ap.add_argument("--serve-grace", type=float, default=30.0,
+                    help="serve: seconds after the window to wait for results")
+    ap.add_argument("--plain-sample", type=int, default=200,
+                    help="serve: requests timed alone for the plain per-request path")
     ap.add_argument("--cpu-budget", type=float, default=15.0,
                     help="seconds of host CPU work for the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -455,6 +462,113 @@ def bench_batched(args, dist: Dist) -> None:
         }), flush=True)
 
 
+SERVE_SEED = 4242
+
+
+def _percentile(v, q):
+    if not v:
+        return None
+    s = sorted(v)
+    return s[min(len(s) - 1, int(round(q * (len(s) - 1))))]
+
+
+def bench_serve(args, dist: Dist) -> None:
+    """Serving: open-loop Poisson arrivals at --rate req/s for --duration s,
+    70% solve-one / 30% solve-all, drawn from the batched-mix distribution,
+    through the two-lane continuous-batching server.  Latency = submit to
+    result.  The plain per-request path (one request at a time, FIFO) is
+    measured on a sample of the same stream and run through the same arrival
+    times."""
+    import random
+
+    from d4gb import engine as E
+    from d4gb.problem import batched_instance, verify_tiling
+
+    rng = random.Random(SERVE_SEED)
+    n = int(args.rate * args.duration)
+    t, arrivals = 0.0, []
+    for _ in range(n):
+        t += rng.expovariate(args.rate)
+        arrivals.append(t)
+    probs = [batched_instance(rng, i) for i in range(n)]
+    modes = [E.MODE_SOLVE_ONE if rng.random() < 0.7 else E.MODE_COUNT for _ in range(n)]
+
+    srv = E.Server(device=dist.local_rank, max_states=args.max_states, beam=args.beam)
+    results = {}
+    t0 = time.perf_counter()
+    for i, (p, m, ta) in enumerate(zip(probs, modes, arrivals)):
+        while True:
+            now = time.perf_counter() - t0
+            if now >= ta:
+                break
+            for r in srv.poll():
+                results[r["tag"]] = r
+            time.sleep(min(ta - now, 0.0005))
+        srv.submit(p, m, i)
+    window = time.perf_counter() - t0
+    deadline = t0 + args.duration + args.serve_grace
+    while len(results) < n and time.perf_counter() < deadline:
+        for r in srv.poll():
+            results[r["tag"]] = r
+        time.sleep(0.002)
+    elapsed = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    done = [r for r in results.values() if r["status"] == 0]
+    bad = sum(1 for r in done if r["found"] and
+              not verify_tiling(probs[r["tag"]], r["grid"], r["steps"]))
+    if bad:
+        raise RuntimeError(f"{bad} served solve-one tilings fail the cover check")
+    lat = [r["latency_ms"] for r in done]
+    in_window = sum(1 for r in done if r["latency_ms"] / 1e3 + arrivals[r["tag"]] <= args.duration)
+
+    # Plain path: service time of each sampled request alone (sequential
+    # batch_run), then a FIFO single-server queue over the same arrivals.
+    k = min(n, args.plain_sample)
+    svc = []
+    for i in range(k):
+        a = time.perf_counter()
+        E.batch_run([probs[i]], mode=modes[i], sequential=True, device=dist.local_rank,
+                    max_states=args.max_states, beam=args.beam)
+        svc.append(time.perf_counter() - a)
+    # The queue runs over every arrival of the window; request i takes the
+    # measured service time of sample i mod k.
+    free_at, plain_lat = 0.0, []
+    for i in range(n):
+        start = max(arrivals[i], free_at)
+        free_at = start + svc[i % k]
+        plain_lat.append((free_at - arrivals[i]) * 1e3)
+    plain_rate = k / sum(svc)
+    plain_done_in_window = sum(1 for i in range(n)
+                               if arrivals[i] + plain_lat[i] / 1e3 <= args.duration)
+
+    if dist.rank == 0:
+        print(json.dumps({
+            "metric": "served puzzles/s (Poisson arrivals, 70% solve-one / 30% solve-all)",
+            "value": len(done) / elapsed,
+            "unit": "puzzles/s",
+            "n_gpus": dist.world,
+            "config": {"workload": f"serving: Poisson {args.rate:g} req/s for {args.duration:g} s, "
+                                   f"batched-mix distribution, seed {SERVE_SEED}",
+                       "max_states_per_row": args.max_states, "beam": args.beam},
+            "offered": n, "completed": len(done), "completed_in_window": in_window,
+            "failed": sum(1 for r in results.values() if r["status"] != 0),
+            "unfinished": n - len(results), "elapsed_s": elapsed, "submit_window_s": window,
+            "latency_ms": {"p50": _percentile(lat, 0.5), "p99": _percentile(lat, 0.99)},
+            "frontier_states_per_s": st["states_out"] / elapsed,
+            "server": st,
+            "plain": {"sample": k, "puzzles_per_s": plain_rate,
+                      "completed_in_window": plain_done_in_window,
+                      "latency_ms": {"p50": _percentile(plain_lat, 0.5),
+                                     "p99": _percentile(plain_lat, 0.99)},
+                      "how": "service time of sampled requests alone (one at a time through "
+                             "d4e_batch_run sequential), FIFO single-server queue over all "
+                             "arrivals of the window, sample times reused cyclically"},
+            "speedup_vs_plain": (len(done) / elapsed) / plain_rate,
+            "cover_checked": sum(1 for r in done if r["found"]),
+        }), flush=True)
+
+
 def main() -> None:
     args = parse_args()
     dist = Dist(args.gpus)
@@ -463,6 +577,8 @@ def main() -> None:
             bench_reference(args, dist)
         elif args.workload in ("batched", "batched_one"):
             bench_batched(args, dist)
+        elif args.workload == "serve":
+            bench_serve(args, dist)
         else:
             bench_ours(args, dist)
     finally:

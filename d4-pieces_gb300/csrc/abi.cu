@@ -344,6 +344,10 @@ static void fill_stats(const d4e::Engine &e, d4e_stats *st, bool add = false) {
     st->splits += t.splits;
     st->failed += t.failed;
     st->restarts += t.restarts;
+    st->step_wall_ms += t.step_wall_ms;
+    st->upload_ms += t.upload_ms;
+    st->keep_ms += t.keep_ms;
+    st->trace_ms += t.trace_ms;
 }
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st) {

@@ -65,6 +65,8 @@ struct InstDesc {
     uint32_t dyn_bits;    // width * (max piece rows - 1): window bits a K64 key keeps
     uint32_t used_bits;
     uint32_t flags;       // kInstWitness: records carry a parent witness, not a count
+    uint32_t limit;       // distinct children per row beyond which the instance fails
+                          // (0 = none): k_expand stops expanding it once passed
     uint16_t col_off[kMaxWidth];   // placements anchored at column c: [col_off, col_off + col_len)
     uint16_t col_len[kMaxWidth];
     // Candidate filters (bitsets over a column's placements, `fwords` u64

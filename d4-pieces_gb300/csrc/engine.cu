@@ -2,6 +2,7 @@
 #include "engine.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 
 #include "kernels.h"
@@ -18,26 +19,42 @@ void cuda_check(cudaError_t e, const char *what) {
 }
 
 template <class T>
-void DevBuf<T>::reserve(size_t n, cudaStream_t s, size_t keep) {
+void DevBuf<T>::reserve(size_t n, cudaStream_t stream, size_t keep) {
     if (n <= cap)
         return;
     size_t nc = std::max(n, cap + cap / 2);
     T *np = nullptr;
-    if (cudaMalloc(&np, nc * sizeof(T)) != cudaSuccess) {
+    if (cudaMallocAsync(reinterpret_cast<void **>(&np), nc * sizeof(T), stream) != cudaSuccess) {
         // Geometric growth did not fit: take exactly what is needed.
         cudaGetLastError();
         nc = n;
-        cuda_check(cudaMalloc(&np, nc * sizeof(T)), "cudaMalloc");
+        cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&np), nc * sizeof(T), stream),
+                   "cudaMallocAsync");
     }
     if (p) {
         if (keep)
-            cuda_check(cudaMemcpyAsync(np, p, keep * sizeof(T), cudaMemcpyDeviceToDevice, s),
+            cuda_check(cudaMemcpyAsync(np, p, keep * sizeof(T), cudaMemcpyDeviceToDevice, stream),
                        "cudaMemcpyAsync");
-        cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
-        cudaFree(p);
+        cuda_check(cudaFreeAsync(p, s), "cudaFreeAsync");
     }
     p = np;
     cap = nc;
+    s = stream;
+}
+
+size_t device_available_bytes(int device, size_t *total) {
+    size_t free_b = 0, total_b = 0;
+    cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+    cudaMemPool_t pool;
+    cuda_check(cudaDeviceGetDefaultMemPool(&pool, device), "cudaDeviceGetDefaultMemPool");
+    uint64_t reserved = 0, used = 0;
+    cuda_check(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved),
+               "cudaMemPoolGetAttribute");
+    cuda_check(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used),
+               "cudaMemPoolGetAttribute");
+    if (total)
+        *total = total_b;
+    return free_b + (reserved > used ? reserved - used : 0);
 }
 
 template struct DevBuf<Plc>;
@@ -52,6 +69,8 @@ template struct DevBuf<CopyRange>;
 template struct DevBuf<TraceJob>;
 template struct DevBuf<LevelPtr>;
 template struct DevBuf<TraceOut>;
+template struct DevBuf<TraceChain>;
+template struct DevBuf<TraceSeg>;
 
 namespace {
 
@@ -72,6 +91,10 @@ struct DeviceGuard {
 
 uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
 
+// Placement + filter table bytes of one k_expand launch's instances: about
+// a third of the 129 MB L2, leaving the rest to the hash table's hot lines.
+constexpr uint64_t kGroupTableBytes = 48ull << 20;
+
 uint32_t bit_length(uint64_t v) {
     uint32_t b = 0;
     while (v) {
@@ -91,7 +114,21 @@ Engine::Engine(const EngineOpts &opts) : opts_(opts) {
     DeviceGuard g(opts_.device);
     cuda_check(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, opts_.device),
                "cudaDeviceGetAttribute");
-    cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    {
+        // Freed blocks stay in the device's default pool for the next
+        // growth instead of going back to the driver at every sync.
+        cudaMemPool_t pool;
+        cuda_check(cudaDeviceGetDefaultMemPool(&pool, opts_.device), "cudaDeviceGetDefaultMemPool");
+        uint64_t keep_all = ~0ull;
+        cuda_check(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep_all),
+                   "cudaMemPoolSetAttribute");
+    }
+    int prio_least = 0, prio_greatest = 0;
+    cuda_check(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest),
+               "cudaDeviceGetStreamPriorityRange");
+    cuda_check(cudaStreamCreateWithPriority(&stream_, cudaStreamNonBlocking,
+                                            opts_.high_priority ? prio_greatest : prio_least),
+               "cudaStreamCreate");
     for (auto &e : ev_)
         cuda_check(cudaEventCreate(&e), "cudaEventCreate");
     for (auto &e : ev_run_)
@@ -122,13 +159,13 @@ Engine::~Engine() {
     }
     if (stream_)
         cudaStreamSynchronize(stream_);
-    if (pool_)
-        cudaMemPoolDestroy(pool_);
     ranges_.release();
     keep_max_.release();
     jobs_.release();
     lvlptr_.release();
     trace_out_.release();
+    chain_.release();
+    tsegs_.release();
     for (auto p : lvl_keys_)
         cudaFree(p);
     for (auto p : lvl_cnts_)
@@ -238,6 +275,7 @@ uint32_t Engine::add(const InstanceSpec &sp) {
     in.root_window = w0;
 
     d.flags = sp.mode == Mode::SolveOne ? kInstWitness : 0u;
+    d.limit = (uint32_t)std::min<uint64_t>(sp.max_states, 0xFFFFFFFFull);
     if (reuse) {
         free_ids_.pop_back();
         inst_[id] = std::move(in);
@@ -441,8 +479,8 @@ uint64_t Engine::table_capacity(uint64_t want) {
     const uint64_t slot_bytes = slot_units() * sizeof(ulonglong2);
     if (want * slot_units() <= table_.cap)
         return want;
-    size_t free_b = 0, total_b = 0;
-    cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+    size_t total_b = 0;
+    const size_t free_b = device_available_bytes(opts_.device, &total_b);
     // Each slot is paired with room for load * rec_bytes of next frontier,
     // so the bound does not depend on `want`.
     const double rec_bytes = k64_ ? 16.0 : 24.0;
@@ -460,10 +498,24 @@ int Engine::expand_occupancy() {
                    "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
         occ = std::max(occ, 1);
     }
-    return occ;
+    return opts_.expand_ctas_per_sm > 0 ? std::min(occ, opts_.expand_ctas_per_sm) : occ;
 }
 
+namespace {
+using HostClock = std::chrono::steady_clock;
+double host_ms_since(HostClock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(HostClock::now() - t0).count();
+}
+}  // namespace
+
 StepStats Engine::step() {
+    const auto t_step = HostClock::now();
+    StepStats st = step_impl();
+    tot_.step_wall_ms += host_ms_since(t_step);
+    return st;
+}
+
+StepStats Engine::step_impl() {
     DeviceGuard g(opts_.device);
     StepStats st;
     fix_key_mode();
@@ -471,6 +523,7 @@ StepStats Engine::step() {
         cuda_check(cudaEventRecord(ev_run_[0], stream_), "cudaEventRecord");
         run_started_ = true;
     }
+    const auto t_up = HostClock::now();
     flush_uploads();
 
     // Inject root states of newly added instances as new frontier segments.
@@ -527,6 +580,7 @@ StepStats Engine::step() {
         pending_.clear();
         keep_levels_of(roots);   // level 0 of solve-one instances
     }
+    tot_.upload_ms += host_ms_since(t_up);
     if (n_active_ == 0)
         return st;
 
@@ -551,8 +605,8 @@ StepStats Engine::step() {
     const int nxt_buf = 1 - cur_;
     double mem = 0;
     {
-        size_t free_b = 0, total_b = 0;
-        cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+        size_t total_b = 0;
+        const size_t free_b = device_available_bytes(opts_.device, &total_b);
         mem = memory_limit((double)free_b + (double)table_.cap * sizeof(ulonglong2) +
                            (double)frontier_bytes(nxt_buf) - 0.1 * (double)total_b);
     }
@@ -584,24 +638,33 @@ StepStats Engine::step() {
     for (uint32_t id : run)
         st.n_in += inst_[id].seg_len;
 
-    // Split the running instances into groups whose estimated children fit
-    // the table budget; each group is one k_expand + k_compact pair.
-    // Usually one group holds them all.
+    // Split the running instances into groups, each one k_expand + k_compact
+    // pair: a group's estimated children must fit the table budget, and its
+    // placement and filter tables (read at every walk step) must stay well
+    // inside L2, so that batches of thousands of instances run as a few
+    // cache-resident launches rather than one launch that misses L2 on
+    // every table read.  Usually one group holds them all.
     const double table_mem = std::max(mem - run_front - paused_bytes, run_table);
     const uint64_t budget_slots = (uint64_t)(table_mem / (double)slot_bytes);
     std::vector<std::vector<uint32_t>> groups(1);
     {
-        double acc = 0;
+        double acc = 0, acc_tab = 0;
         for (uint32_t id : run) {
             const Inst &in = inst_[id];
             const double e = (double)std::max<uint64_t>(in.seg_len, 1) * in.growth /
                              opts_.target_load;
-            if (!groups.back().empty() && acc + e > (double)budget_slots) {
+            const double tab = (double)(in.lib.plc.size() * sizeof(Plc) +
+                                        in.lib.filters.size() * sizeof(unsigned long long) +
+                                        sizeof(InstDesc));
+            if (!groups.back().empty() &&
+                (acc + e > (double)budget_slots || acc_tab + tab > (double)kGroupTableBytes)) {
                 groups.emplace_back();
                 acc = 0;
+                acc_tab = 0;
             }
             groups.back().push_back(id);
             acc += e;
+            acc_tab += tab;
         }
     }
 
@@ -993,8 +1056,12 @@ StepStats Engine::step() {
     cur_ = nxt;
     // Solve-one: keep the new levels, trace the instances that completed
     // their last row, and retry exhausted sampled attempts wider.
+    const auto t_keep = HostClock::now();
     keep_levels_of(keep_now);
+    const auto t_trace = HostClock::now();
+    tot_.keep_ms += host_ms_since(t_keep);
     trace_solutions(to_trace);
+    tot_.trace_ms += host_ms_since(t_trace);
     for (uint32_t id : ended) {
         if (inst_[id].sampled)
             restart(id);
@@ -1023,25 +1090,15 @@ void Engine::keep_levels_of(const std::vector<uint32_t> &ids) {
         total += inst_[id].seg_len;
     if (ids.empty() || total == 0)
         return;
-    if (!pool_) {
-        cudaMemPoolProps props{};
-        props.allocType = cudaMemAllocationTypePinned;
-        props.location.type = cudaMemLocationTypeDevice;
-        props.location.id = opts_.device;
-        cuda_check(cudaMemPoolCreate(&pool_, &props), "cudaMemPoolCreate");
-        uint64_t keep_all = ~0ull;
-        cuda_check(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep_all),
-                   "cudaMemPoolSetAttribute");
-    }
     LvlChunk ch;
-    cuda_check(cudaMallocFromPoolAsync(reinterpret_cast<void **>(&ch.keys),
-                                       total * sizeof(ulonglong2), pool_, stream_),
-               "cudaMallocFromPoolAsync");
+    cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&ch.keys), total * sizeof(ulonglong2),
+                               stream_),
+               "cudaMallocAsync");
     ch.bytes = total * sizeof(ulonglong2);
     if (!k64_) {
-        cuda_check(cudaMallocFromPoolAsync(reinterpret_cast<void **>(&ch.cnts),
-                                           total * sizeof(unsigned long long), pool_, stream_),
-                   "cudaMallocFromPoolAsync");
+        cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&ch.cnts),
+                                   total * sizeof(unsigned long long), stream_),
+                   "cudaMallocAsync");
         ch.bytes += total * sizeof(unsigned long long);
     }
     uint32_t ci;
@@ -1145,20 +1202,65 @@ void Engine::trace_solutions(const std::vector<uint32_t> &ids) {
             lp.push_back({c.keys + l.first, c.cnts ? c.cnts + l.first : nullptr, l.len});
         }
     }
+    // Flattened passes: the final level of every job (passes 0 and 1),
+    // then level H - s of every job with H >= s, for s = 1, 2, ...
+    uint32_t hmax = 0;
+    for (const TraceJob &j : jobs)
+        hmax = std::max(hmax, j.height);
+    std::vector<TraceSeg> segs;
+    std::vector<std::pair<size_t, unsigned long long>> pass_at;   // (first seg, records)
+    for (uint32_t s = 0; s <= hmax; s++) {
+        const size_t first = segs.size();
+        unsigned long long base = 0;
+        for (uint32_t k = 0; k < jobs.size(); k++) {
+            if (jobs[k].height < s)
+                continue;
+            const uint32_t r = jobs[k].height - s;
+            const unsigned long long len = lp[jobs[k].lvl + r].len;
+            if (!len)
+                continue;
+            segs.push_back({k, r, base, len});
+            base += len;
+        }
+        pass_at.push_back({first, base});
+    }
     jobs_.reserve(jobs.size(), stream_);
     lvlptr_.reserve(lp.size(), stream_);
     trace_out_.reserve(jobs.size(), stream_);
+    chain_.reserve(jobs.size(), stream_);
+    tsegs_.reserve(std::max<size_t>(segs.size(), 1), stream_);
     cuda_check(cudaMemcpyAsync(jobs_.p, jobs.data(), jobs.size() * sizeof(TraceJob),
                                cudaMemcpyHostToDevice, stream_),
                "upload trace jobs");
     cuda_check(cudaMemcpyAsync(lvlptr_.p, lp.data(), lp.size() * sizeof(LevelPtr),
                                cudaMemcpyHostToDevice, stream_),
                "upload level pointers");
-    tot_.h2d_bytes += jobs.size() * sizeof(TraceJob) + lp.size() * sizeof(LevelPtr);
+    if (!segs.empty())
+        cuda_check(cudaMemcpyAsync(tsegs_.p, segs.data(), segs.size() * sizeof(TraceSeg),
+                                   cudaMemcpyHostToDevice, stream_),
+                   "upload trace segments");
+    cuda_check(cudaMemsetAsync(chain_.p, 0, jobs.size() * sizeof(TraceChain), stream_), "memset");
+    tot_.h2d_bytes += jobs.size() * sizeof(TraceJob) + lp.size() * sizeof(LevelPtr) +
+                      segs.size() * sizeof(TraceSeg);
+    auto pass = [&](int kind, uint32_t s) {
+        const size_t first = pass_at[s].first;
+        const size_t nseg = (s + 1 < pass_at.size() ? pass_at[s + 1].first : segs.size()) - first;
+        const unsigned long long total = pass_at[s].second;
+        const int grid = (int)std::min<unsigned long long>((total + 255) / 256,
+                                                           (unsigned long long)sms_ * 8);
+        launch_trace_pass(k64_, kind, lvlptr_.p, jobs_.p, tsegs_.p + first, (uint32_t)nseg, total,
+                          chain_.p, std::max(grid, 1), stream_);
+        cuda_check(cudaGetLastError(), "k_trace_pass launch");
+        tot_.other_launches++;
+    };
+    pass(0, 0);
+    pass(1, 0);
+    for (uint32_t s = 1; s <= hmax; s++)
+        pass(2, s);
     const int grid = (int)std::min<uint64_t>((jobs.size() + 7) / 8, (uint64_t)sms_ * 8);
-    launch_trace(k64_, insts_.p, plc_.p, lvlptr_.p, jobs_.p, (uint32_t)jobs.size(), trace_out_.p,
-                 grid, stream_);
-    cuda_check(cudaGetLastError(), "k_trace launch");
+    launch_trace_fill(k64_, insts_.p, plc_.p, lvlptr_.p, jobs_.p, (uint32_t)jobs.size(), chain_.p,
+                      trace_out_.p, grid, stream_);
+    cuda_check(cudaGetLastError(), "k_trace_fill launch");
     tot_.other_launches++;
     std::vector<TraceOut> out(jobs.size());
     cuda_check(cudaMemcpyAsync(out.data(), trace_out_.p, out.size() * sizeof(TraceOut),

@@ -39,24 +39,31 @@ enum ErrCode : int {
 
 void cuda_check(cudaError_t e, const char *what);
 
-// Grow-only device buffer.
+// Grow-only device buffer, allocated stream-ordered (cudaMallocAsync /
+// cudaFreeAsync on the owner's stream) so that growing it never
+// synchronises the device: engines on other streams keep running.
 template <class T>
 struct DevBuf {
     T *p = nullptr;
     size_t cap = 0;
+    cudaStream_t s = nullptr;   // stream of the last allocation
     DevBuf() = default;
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
     ~DevBuf() { release(); }
     void release() {
         if (p)
-            cudaFree(p);
+            cudaFreeAsync(p, s);
         p = nullptr;
         cap = 0;
     }
     // Ensures capacity >= n elements; keeps the first `keep` elements.
     void reserve(size_t n, cudaStream_t s, size_t keep = 0);
 };
+
+// Device bytes an allocation can still get: free memory plus what the
+// device's stream-ordered pools hold in reserve.
+size_t device_available_bytes(int device, size_t *total);
 
 enum class KeyMode { Auto, K64, K128 };
 
@@ -78,6 +85,10 @@ struct EngineOpts {
     // (0 = layout chosen from the instances, see fix_key_mode).  Instances
     // whose window + counter bits exceed 63 - k64_inst_bits are rejected.
     uint32_t k64_inst_bits = 0;
+    // k_expand CTAs per SM (0 = as many as fit).  A lower value leaves room
+    // on every SM for kernels of another engine running concurrently.
+    int expand_ctas_per_sm = 0;
+    bool high_priority = false;    // create the engine's stream at the highest priority
 };
 
 enum class Mode : uint32_t { Count = 0, SolveOne = 1 };
@@ -114,6 +125,10 @@ struct Totals {
     uint64_t peak_frontier = 0;
     uint64_t h2d_bytes = 0, d2h_bytes = 0;
     double run_ms = 0.0;           // CUDA-event time from the first step to the last
+    // Host wall time inside step(), and the parts spent uploading new
+    // instances, keeping solve-one levels and tracing solve-one tilings
+    // (each including the device work it waits for).
+    double step_wall_ms = 0.0, upload_ms = 0.0, keep_ms = 0.0, trace_ms = 0.0;
 };
 
 // One kept frontier level of a solve-one instance: `len` records from
@@ -204,6 +219,7 @@ private:
         std::vector<int16_t> sgrid;
     };
 
+    StepStats step_impl();
     void ensure_inst_capacity(size_t n);
     void fail_instance(uint32_t id, int code, const std::string &msg);
     // Solve-one support: kept levels, tracing, restarts with a wider sample.
@@ -271,8 +287,8 @@ private:
     std::vector<unsigned long long *> lvl_cnts_;
     std::vector<uint64_t> lvl_n_;
 
-    // Kept levels of solve-one instances: one block per step from a stream-
-    // ordered pool, freed when no instance refers to it any more.
+    // Kept levels of solve-one instances: one block per step, allocated
+    // stream-ordered, freed when no instance refers to it any more.
     struct LvlChunk {
         ulonglong2 *keys = nullptr;
         unsigned long long *cnts = nullptr;
@@ -282,13 +298,14 @@ private:
     std::vector<LvlChunk> chunks_;
     std::vector<uint32_t> free_chunks_;
     uint64_t lvl_bytes_ = 0;
-    cudaMemPool_t pool_ = nullptr;
     DevBuf<CopyRange> ranges_;
     DevBuf<unsigned long long> keep_max_;
     std::vector<unsigned long long> h_keep_max_;
     DevBuf<TraceJob> jobs_;
     DevBuf<LevelPtr> lvlptr_;
     DevBuf<TraceOut> trace_out_;
+    DevBuf<TraceChain> chain_;
+    DevBuf<TraceSeg> tsegs_;
 
     Totals tot_;
     bool run_started_ = false;

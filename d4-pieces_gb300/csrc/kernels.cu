@@ -288,8 +288,10 @@ struct WarpStage {
     uint32_t inst[kStage];
 };
 
+// Returns true (warp-uniform) once the table has overflowed anywhere: the
+// level is redone with a larger table, so the expansion stops at once.
 template <bool K64>
-__device__ __forceinline__ void flush_children(const ExpandArgs &a, const WarpStage &ws, int base,
+__device__ __forceinline__ bool flush_children(const ExpandArgs &a, const WarpStage &ws, int base,
                                                int n, unsigned lane) {
     // Lane i inserts child base + i: up to 32 independent inserts in flight.
     int r = 2;
@@ -306,13 +308,19 @@ __device__ __forceinline__ void flush_children(const ExpandArgs &a, const WarpSt
             r = insert128(static_cast<Slot32 *>(a.table), a.cap, ws.k0[j], ws.k1[j], ws.cnt[j],
                           a.max_probe, wmax);
     }
-    if (__any_sync(0xffffffffu, r < 0) && lane == 0)
+    const bool over = __any_sync(0xffffffffu, r < 0);
+    if (over && lane == 0)
         atomicOr(a.status, kStatusTableOverflow);
     // New keys per instance, aggregated over the lanes sharing an instance.
     const bool fresh = r == 1;
     const unsigned peers = __match_any_sync(0xffffffffu, fresh ? inst : 0xFFFFFFFFu);
     if (fresh && lane == (unsigned)(__ffs(peers) - 1))
         atomicAdd(&a.inst_unique[inst], (unsigned)__popc(peers));
+    unsigned int stt = 0;
+    if (lane == 0)
+        stt = __ldcg(a.status);
+    stt = __shfl_sync(0xffffffffu, stt, 0);
+    return over || (stt & kStatusTableOverflow) != 0u;
 }
 
 // Expansion.  Warps work independently (no block barrier): each warp takes
@@ -361,10 +369,14 @@ k_expand(ExpandArgs a) {
         while (need && !no_more) {
             if (c_next >= c_end) {
                 unsigned long long ci = 0;
-                if (lane == 0)
+                unsigned int stt = 0;
+                if (lane == 0) {
                     ci = atomicAdd(a.work, 1ull);
+                    stt = __ldcg(a.status);
+                }
                 ci = __shfl_sync(0xffffffffu, ci, 0);
-                if (ci >= a.n_chunks) {
+                stt = __shfl_sync(0xffffffffu, stt, 0);
+                if (ci >= a.n_chunks || (stt & kStatusTableOverflow)) {
                     no_more = true;
                     break;
                 }
@@ -382,6 +394,11 @@ k_expand(ExpandArgs a) {
                 c_next = s.begin + (ci - s.chunk_base) * a.chunk_states;
                 const unsigned long long se = s.begin + s.len;
                 c_end = c_next + a.chunk_states < se ? c_next + a.chunk_states : se;
+                // An instance past its frontier limit fails anyway: skip the
+                // rest of its work.
+                const uint32_t lim = a.insts[s.inst].limit;
+                if (lim && __ldcg(a.inst_unique + s.inst) > lim)
+                    c_next = c_end;
             }
             const unsigned long long avail = c_end - c_next;
             const unsigned take = (unsigned)(avail < (unsigned long long)__popc(need)
@@ -600,9 +617,13 @@ k_expand(ExpandArgs a) {
         nbuf += __popc(em);
         if (nbuf >= 32) {
             __syncwarp();
-            flush_children<K64>(a, ws, nbuf - 32, 32, lane);
+            const bool over = flush_children<K64>(a, ws, nbuf - 32, 32, lane);
             nbuf -= 32;
             __syncwarp();
+            if (over) {
+                nbuf = 0;   // the level is redone: drop the rest
+                break;
+            }
         }
     }
     if (nbuf > 0) {

@@ -129,13 +129,39 @@ struct TraceOut {
     uint16_t plc[kMaxHeight][kMaxWidth];   // instance-relative placement indices
 };
 
-// For every job: pick the final state with the largest identity, follow the
-// parent witnesses back to the root (largest identity among matching
-// parents), then find each row's first fill (depth-first order) leading
-// from the chosen parent to the chosen child.  One warp per job.
-void launch_trace(bool k64, const InstDesc *insts, const Plc *plc, const LevelPtr *levels,
-                  const TraceJob *jobs, uint32_t n_jobs, TraceOut *out, int grid,
-                  cudaStream_t s);
+// Chosen record per kept level of a job, and the witness it carries.
+struct TraceChain {
+    unsigned long long idx[kMaxHeight + 1];   // chosen record + 1 (0 = none found)
+    unsigned long long tgt[kMaxHeight + 1];   // witness of the chosen record
+    unsigned long long best;                  // largest final-state identity
+};
+
+// Records of one job's level in a flattened pass over many jobs.
+struct TraceSeg {
+    uint32_t job;
+    uint32_t level;                  // level index r of the job
+    unsigned long long base;         // first flattened index
+    unsigned long long len;
+};
+
+// Tracing runs in passes over the kept levels of all jobs at once:
+//   final pass A : best[job] = largest identity among the final states;
+//   final pass B : the final state with that identity is chosen;
+//   level passes : from the final level down, the record of level r whose
+//                  identity equals the witness chosen at level r + 1 (a
+//                  unique state) is chosen;
+//   fill         : per job and row, the first fill (depth-first order)
+//                  leading from the chosen parent to the chosen child.
+// `segs` covers the records of one pass (sorted by base, n_segs entries,
+// `total` records).
+void launch_trace_pass(bool k64, int pass, const LevelPtr *levels, const TraceJob *jobs,
+                       const TraceSeg *segs, uint32_t n_segs, unsigned long long total,
+                       TraceChain *chain, int grid, cudaStream_t s);
+// Per job and row, the first fill (depth-first order) leading from the
+// chosen parent to the chosen child; one warp per job, one lane per row.
+void launch_trace_fill(bool k64, const InstDesc *insts, const Plc *plc, const LevelPtr *levels,
+                       const TraceJob *jobs, uint32_t n_jobs, const TraceChain *chain,
+                       TraceOut *out, int grid, cudaStream_t s);
 
 // Copies record ranges (and K128 counts when cnts are given) between
 // frontier buffers: one warp per range.

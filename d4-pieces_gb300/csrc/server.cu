@@ -1,12 +1,22 @@
 // server.cu -- serving loop: continuous batching of tiling requests on one GPU.
 //
-// A native worker thread owns two engines (packed 64-bit keys for requests
-// that fit them, the general 128-bit encoding for the rest).  Each loop
-// iteration admits queued requests in arrival order while the projected
-// device bytes of everything admitted stay within the budget, then advances
-// every admitted request by one board row (one k_expand + k_compact pair per
-// engine for all of them), then hands out the requests that finished.  A
-// request that arrives while others run joins at their next row.
+// Two lanes, each a native worker thread with its own engines (packed 64-bit
+// keys for requests that fit them, the general 128-bit encoding for the
+// rest) on its own CUDA stream:
+//   fast lane -- every request starts here, with a per-row frontier limit
+//                of kFastStates; high stream priority.
+//   slow lane -- requests whose frontier outgrew the fast lane restart here
+//                from their first row; its k_expand grid leaves one CTA slot
+//                per SM free, so fast-lane kernels run beside it.
+// A heavy request therefore never holds up the rows of the light ones, and
+// both lanes' launches overlap on the device.  Each lane loop admits queued
+// requests in arrival order while the projected device bytes of everything
+// admitted (both lanes) stay within the budget, advances every admitted
+// request by one board row (one k_expand + k_compact pair per engine for
+// all of them), and hands out the requests that finished.  A request that
+// arrives while others run joins at their next row.  A restarted request
+// repeats exactly what it did in the fast lane, so every result is the one
+// the request gets alone.
 //
 // No counterpart in the reference: its SearcherFactory (src/searcher.cpp:86-107)
 // runs a fixed job list, one CudaSearcher per job.
@@ -39,10 +49,14 @@ double ms_between(Clock::time_point a, Clock::time_point b) {
     return std::chrono::duration<double, std::milli>(b - a).count();
 }
 
-// Instance ids of the packed-key engine: 14 bits, so up to 16384 requests
-// on the device at once; requests whose window and counter bits exceed 49
-// use the general engine.
+// Instance ids of the packed-key engines: 14 bits, so up to 16384 requests
+// per lane on the device at once; requests whose window and counter bits
+// exceed 49 use the general engine.
 constexpr uint32_t kServerIdBits = 14;
+
+// Fast-lane limit on one row's distinct states (about 6 MB of frontier and
+// table per request).
+constexpr uint64_t kFastStates = 1ull << 17;
 
 struct Request {
     uint32_t width = 0, height = 0, n_pieces = 0, sym = 0, mode = 0;
@@ -51,7 +65,7 @@ struct Request {
     std::vector<uint32_t> counts;
     uint64_t tag = 0;
     Clock::time_point t_submit, t_admit;
-    double projected = 0;   // bytes charged against the budget at admission
+    bool moved = false;     // restarted in the slow lane
 };
 
 }  // namespace
@@ -60,29 +74,38 @@ class Server {
 public:
     explicit Server(const d4e_server_opts &o) : opts_(o) {
         if (!opts_.max_active)
-            opts_.max_active = 8192;
+            opts_.max_active = 4096;
         opts_.max_active = std::min<uint32_t>(opts_.max_active, 1u << kServerIdBits);
         int n = 0;
         cuda_check(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
         if (opts_.device < 0 || opts_.device >= n)
             throw Error(kErrInvalid, "no such CUDA device");
         cuda_check(cudaSetDevice(opts_.device), "cudaSetDevice");
-        size_t free_b = 0, total_b = 0;
-        cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+        size_t total_b = 0;
+        device_available_bytes(opts_.device, &total_b);
         const uint64_t cap = (uint64_t)((double)total_b * 0.9);
         budget_ = opts_.memory_budget ? opts_.memory_budget
                                       : std::min<uint64_t>(150ull << 30, cap);
-        EngineOpts eo;
-        eo.device = opts_.device;
-        eo.isolate_failures = true;
-        eo.memory_budget = budget_;
-        EngineOpts e64 = eo;
-        e64.k64_inst_bits = kServerIdBits;
-        eng_[0] = std::make_unique<Engine>(e64);
-        EngineOpts e128 = eo;
-        e128.key_mode = KeyMode::K128;
-        eng_[1] = std::make_unique<Engine>(e128);
-        worker_ = std::thread([this] { loop(); });
+        int occ = 0;
+        cuda_check(expand_max_blocks_per_sm(true, &occ), "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        for (int l = 0; l < 2; l++) {
+            Lane &ln = lane_[l];
+            EngineOpts eo;
+            eo.device = opts_.device;
+            eo.isolate_failures = true;
+            eo.memory_budget = budget_;
+            eo.high_priority = l == 0;
+            if (l == 1 && occ > 1)
+                eo.expand_ctas_per_sm = occ - 1;
+            EngineOpts e64 = eo;
+            e64.k64_inst_bits = kServerIdBits;
+            ln.eng[0] = std::make_unique<Engine>(e64);
+            EngineOpts e128 = eo;
+            e128.key_mode = KeyMode::K128;
+            ln.eng[1] = std::make_unique<Engine>(e128);
+        }
+        for (int l = 0; l < 2; l++)
+            lane_[l].worker = std::thread([this, l] { loop(l); });
     }
 
     ~Server() {
@@ -90,9 +113,11 @@ public:
             std::lock_guard<std::mutex> lk(mu_);
             stop_ = true;
         }
-        cv_.notify_all();
-        if (worker_.joinable())
-            worker_.join();
+        for (auto &ln : lane_)
+            ln.cv.notify_all();
+        for (auto &ln : lane_)
+            if (ln.worker.joinable())
+                ln.worker.join();
     }
 
     void submit(const d4e_instance &in, uint32_t mode, uint64_t tag) {
@@ -119,10 +144,10 @@ public:
             std::lock_guard<std::mutex> lk(mu_);
             if (worker_error_)
                 throw Error(worker_code_, worker_msg_);
-            queue_.push_back(std::move(r));
+            lane_[0].queue.push_back(std::move(r));
             st_.submitted++;
         }
-        cv_.notify_all();
+        lane_[0].cv.notify_all();
     }
 
     uint32_t poll(d4e_result *out, uint32_t max) {
@@ -154,54 +179,77 @@ public:
     }
 
 private:
-    // Bytes a running request is expected to hold on its next row.
-    double running_projection(int e, uint32_t id) const {
-        return (double)eng_[e]->projected_bytes(id);
-    }
+    struct Lane {
+        std::unique_ptr<Engine> eng[2];
+        std::thread worker;
+        std::condition_variable cv;
+        std::deque<Request> queue;                            // guarded by mu_
+        std::unordered_map<uint32_t, Request> running[2];     // worker-owned
+        size_t n_running = 0;                                 // guarded by mu_
+        double projected = 0;                                 // guarded by mu_
+        double avg_peak = 0;                                  // worker-owned
+        uint64_t n_peaks = 0;
+    };
 
     // Bytes charged for a request not yet started: solve-one requests are
-    // bounded by their sample width; counting requests are charged the
-    // average peak of the counting requests finished so far.
-    double initial_projection(const Request &r) const {
+    // bounded by their sample width, fast-lane requests by the lane limit;
+    // slow-lane counting requests are charged the average peak of the ones
+    // finished so far.
+    double initial_projection(int l, const Request &r) const {
         const double per_state = 16.0 + 16.0 / 0.5;   // record + table slot at load 0.5
         const double floor_b = 1.0 * 1024 * 1024;
+        double p = l == 0 ? (double)kFastStates * per_state : lane_[l].avg_peak;
         if (r.mode == D4E_MODE_SOLVE_ONE && opts_.beam)
-            return std::max(floor_b, (double)opts_.beam * 64.0 * per_state);
-        return std::max(floor_b, avg_peak_bytes_);
+            p = std::min(p, (double)opts_.beam * 64.0 * per_state);
+        return std::max(floor_b, p);
     }
 
-    void loop() {
+    uint64_t lane_limit(int l) const {
+        if (l == 1)
+            return opts_.max_states;
+        return opts_.max_states ? std::min(opts_.max_states, kFastStates) : kFastStates;
+    }
+
+    void loop(int l) {
+        Lane &ln = lane_[l];
         try {
             cuda_check(cudaSetDevice(opts_.device), "cudaSetDevice");
             for (;;) {
-                admit();
+                admit(l);
                 bool busy = false;
                 for (int e = 0; e < 2; e++) {
-                    if (!eng_[e]->has_active())
+                    if (!ln.eng[e]->has_active())
                         continue;
                     busy = true;
                     const auto t0 = Clock::now();
-                    const StepStats s = eng_[e]->step();
+                    const uint64_t restarts0 = ln.eng[e]->totals().restarts;
+                    const size_t n_run = ln.running[e].size();
+                    const StepStats s = ln.eng[e]->step();
                     const auto t1 = Clock::now();
-                    collect(e);
+                    collect(l, e);
                     std::lock_guard<std::mutex> lk(mu_);
                     st_.steps++;
                     st_.states_out += s.n_out;
                     st_.busy_ms += ms_between(t0, t1);
+                    st_.lane_steps[l]++;
+                    st_.lane_busy_ms[l] += ms_between(t0, t1);
+                    st_.lane_kernel_ms[l] += s.expand_ms + s.compact_ms;
+                    st_.lane_inst_rows[l] += n_run - s.paused;
+                    st_.restarts += ln.eng[e]->totals().restarts - restarts0;
+                    st_.paused += s.paused;
                 }
-                if (!busy) {
-                    std::unique_lock<std::mutex> lk(mu_);
-                    if (stop_)
-                        return;
-                    if (queue_.empty())
-                        cv_.wait(lk, [&] { return stop_ || !queue_.empty(); });
-                    if (stop_)
-                        return;
-                } else {
-                    std::lock_guard<std::mutex> lk(mu_);
-                    if (stop_)
-                        return;
-                }
+                double proj = 0;
+                for (int e = 0; e < 2; e++)
+                    for (const auto &[id, r] : ln.running[e])
+                        proj += (double)ln.eng[e]->projected_bytes(id);
+                std::unique_lock<std::mutex> lk(mu_);
+                ln.projected = proj;
+                if (stop_)
+                    return;
+                if (!busy && ln.queue.empty())
+                    ln.cv.wait(lk, [&] { return stop_ || !ln.queue.empty(); });
+                if (stop_)
+                    return;
             }
         } catch (const Error &e) {
             std::lock_guard<std::mutex> lk(mu_);
@@ -217,64 +265,57 @@ private:
         done_cv_.notify_all();
     }
 
-    // Admission: arrival order, while the projected bytes of the running
-    // requests plus the candidate fit the budget (the first request always
-    // fits) and fewer than max_active run.
-    void admit() {
-        std::deque<Request> take;
+    // Admission: arrival order, while the projected bytes of the requests on
+    // the device (both lanes) plus the candidate fit the budget (a lane with
+    // nothing running always takes one) and fewer than max_active run.
+    void admit(int l) {
+        Lane &ln = lane_[l];
+        std::vector<Request> take;
         {
             std::lock_guard<std::mutex> lk(mu_);
-            if (queue_.empty())
+            if (ln.queue.empty())
                 return;
-            double proj = 0;
-            for (int e = 0; e < 2; e++)
-                for (const auto &[id, r] : running_[e])
-                    proj += running_projection(e, id);
-            size_t active = running_[0].size() + running_[1].size();
-            while (!queue_.empty() && active < opts_.max_active) {
-                const double p = initial_projection(queue_.front());
+            double proj = lane_[0].projected + lane_[1].projected;
+            size_t active = ln.n_running;
+            const size_t cap = l == 0 ? opts_.max_active : std::max<size_t>(16, opts_.max_active / 16);
+            while (!ln.queue.empty() && active < cap) {
+                const double p = initial_projection(l, ln.queue.front());
                 if (active > 0 && proj + p > (double)budget_)
                     break;
-                take.push_back(std::move(queue_.front()));
-                take.back().projected = p;
-                queue_.pop_front();
+                take.push_back(std::move(ln.queue.front()));
+                ln.queue.pop_front();
                 proj += p;
+                ln.projected += p;
                 active++;
             }
+            ln.n_running = active;
             st_.peak_projected = std::max<uint64_t>(st_.peak_projected, (uint64_t)proj);
         }
         for (Request &r : take) {
-            r.t_admit = Clock::now();
-            d4e_instance in{};
-            in.width = r.width;
-            in.height = r.height;
-            in.rows = r.rows.data();
-            in.n_pieces = r.n_pieces;
-            in.shapes = r.shapes.data();
-            in.counts = r.counts.data();
-            in.sym = r.sym;
+            if (!r.moved)
+                r.t_admit = Clock::now();
             InstanceSpec sp;
-            sp.width = in.width;
-            sp.height = in.height;
-            sp.rows = in.rows;
-            sp.shapes = in.shapes;
-            sp.counts = in.counts;
-            sp.n_pieces = in.n_pieces;
-            sp.sym = in.sym;
+            sp.width = r.width;
+            sp.height = r.height;
+            sp.rows = r.rows.data();
+            sp.shapes = r.shapes.data();
+            sp.counts = r.counts.data();
+            sp.n_pieces = r.n_pieces;
+            sp.sym = r.sym;
             sp.mode = r.mode == D4E_MODE_SOLVE_ONE ? Mode::SolveOne : Mode::Count;
-            sp.max_states = opts_.max_states;
+            sp.max_states = lane_limit(l);
             sp.beam = opts_.beam;
             int e = 0;
             uint32_t id = 0;
             try {
                 try {
-                    id = eng_[0]->add(sp);
+                    id = ln.eng[0]->add(sp);
                 } catch (const Error &err) {
                     if (err.code != kErrUnsupported ||
                         std::string(err.what()).find("packed key") == std::string::npos)
                         throw;
                     e = 1;
-                    id = eng_[1]->add(sp);
+                    id = ln.eng[1]->add(sp);
                 }
             } catch (const Error &err) {
                 // Invalid or unsupported request: it fails on its own.
@@ -285,71 +326,86 @@ private:
                 std::memset(res.grid, -1, sizeof(res.grid));
                 std::memset(res.steps, -1, sizeof(res.steps));
                 res.queued_ms = ms_between(r.t_submit, r.t_admit);
-                res.latency_ms = res.queued_ms;
+                res.latency_ms = ms_between(r.t_submit, Clock::now());
                 std::lock_guard<std::mutex> lk(mu_);
+                ln.n_running--;
                 results_.push_back(res);
                 st_.failed++;
                 done_cv_.notify_all();
                 continue;
             }
+            ln.running[e].emplace(id, std::move(r));
             std::lock_guard<std::mutex> lk(mu_);
-            running_[e].emplace(id, std::move(r));
             st_.admitted++;
             st_.peak_active = std::max<uint64_t>(st_.peak_active,
-                                                 running_[0].size() + running_[1].size());
+                                                 lane_[0].n_running + lane_[1].n_running);
         }
     }
 
-    void collect(int e) {
-        Engine &eng = *eng_[e];
+    void collect(int l, int e) {
+        Lane &ln = lane_[l];
+        Engine &eng = *ln.eng[e];
         std::vector<uint32_t> fin;
-        for (const auto &[id, r] : running_[e])
+        for (const auto &[id, r] : ln.running[e])
             if (eng.done(id))
                 fin.push_back(id);
         if (fin.empty())
             return;
         eng.sync_results();
         const auto now = Clock::now();
-        std::vector<d4e_result> out(fin.size());
-        for (size_t k = 0; k < fin.size(); k++) {
-            const uint32_t id = fin[k];
-            const Request &r = running_[e].at(id);
-            d4e_result &res = out[k];
-            engine_result(eng, id, r.mode, &res);
-            res.tag = r.tag;
-            res.queued_ms = ms_between(r.t_submit, r.t_admit);
-            res.latency_ms = ms_between(r.t_submit, now);
-            if (r.mode == D4E_MODE_COUNT && res.status == 0) {
-                const double peak = (double)eng.peak_bytes(id);
-                avg_peak_bytes_ = n_peaks_ ? 0.95 * avg_peak_bytes_ + 0.05 * peak : peak;
-                n_peaks_++;
+        std::vector<d4e_result> out;
+        std::vector<Request> moved;
+        for (uint32_t id : fin) {
+            Request &r = ln.running[e].at(id);
+            // Outgrew the fast lane (and not the caller's own limit):
+            // restart in the slow lane.
+            if (l == 0 && eng.status(id) == kErrUnsupported &&
+                eng.error(id).rfind("frontier limit exceeded", 0) == 0 &&
+                (opts_.max_states == 0 || opts_.max_states > kFastStates)) {
+                r.moved = true;
+                moved.push_back(std::move(r));
+            } else {
+                d4e_result res;
+                engine_result(eng, id, r.mode, &res);
+                res.tag = r.tag;
+                res.queued_ms = ms_between(r.t_submit, r.t_admit);
+                res.latency_ms = ms_between(r.t_submit, now);
+                if (r.mode == D4E_MODE_COUNT && res.status == 0) {
+                    const double peak = (double)eng.peak_bytes(id);
+                    ln.avg_peak = ln.n_peaks ? 0.95 * ln.avg_peak + 0.05 * peak : peak;
+                    ln.n_peaks++;
+                }
+                out.push_back(res);
             }
+            ln.running[e].erase(id);
             eng.release(id);
         }
-        std::lock_guard<std::mutex> lk(mu_);
-        for (size_t k = 0; k < fin.size(); k++) {
-            running_[e].erase(fin[k]);
-            results_.push_back(out[k]);
-            if (out[k].status)
-                st_.failed++;
-            else
-                st_.completed++;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            ln.n_running -= fin.size();
+            for (const d4e_result &res : out) {
+                results_.push_back(res);
+                if (res.status)
+                    st_.failed++;
+                else
+                    st_.completed++;
+            }
+            for (Request &r : moved)
+                lane_[1].queue.push_back(std::move(r));
+            st_.moved += moved.size();
         }
+        if (!moved.empty())
+            lane_[1].cv.notify_all();
         done_cv_.notify_all();
     }
 
     d4e_server_opts opts_;
     uint64_t budget_ = 0;
-    std::unique_ptr<Engine> eng_[2];
-    std::thread worker_;
+    Lane lane_[2];
     std::mutex mu_;
-    std::condition_variable cv_, done_cv_;
-    std::deque<Request> queue_;
-    std::unordered_map<uint32_t, Request> running_[2];   // by engine instance id
+    std::condition_variable done_cv_;
     std::deque<d4e_result> results_;
     d4e_server_stats st_{};
-    double avg_peak_bytes_ = 0;
-    uint64_t n_peaks_ = 0;
     bool stop_ = false;
     bool worker_error_ = false;
     int worker_code_ = 0;

@@ -65,6 +65,10 @@ class Stats(C.Structure):
         ("splits", C.c_uint64),
         ("failed", C.c_uint64),
         ("restarts", C.c_uint64),
+        ("step_wall_ms", C.c_double),
+        ("upload_ms", C.c_double),
+        ("keep_ms", C.c_double),
+        ("trace_ms", C.c_double),
     ]
 
     def as_dict(self) -> dict:
@@ -129,10 +133,18 @@ class ServerStats(C.Structure):
         ("peak_projected", C.c_uint64),
         ("states_out", C.c_uint64),
         ("busy_ms", C.c_double),
+        ("moved", C.c_uint64),
+        ("lane_steps", C.c_uint64 * 2),
+        ("lane_busy_ms", C.c_double * 2),
+        ("lane_kernel_ms", C.c_double * 2),
+        ("lane_inst_rows", C.c_uint64 * 2),
+        ("restarts", C.c_uint64),
+        ("paused", C.c_uint64),
     ]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: (list(v) if not isinstance(v := getattr(self, k), (int, float)) else v)
+                for k, _ in self._fields_}
 
 
 class Instance(C.Structure):
@@ -411,7 +423,7 @@ class Server:
         self._shape[tag] = (problem.width, problem.height)
         _check(_lib.d4e_server_submit(self._h, arr, mode, tag))
 
-    def poll(self, max_results: int = 4096):
+    def poll(self, max_results: int = 256):
         out = (Result * max_results)()
         n = C.c_uint32()
         _check(_lib.d4e_server_poll(self._h, out, max_results, C.byref(n)))

@@ -18,6 +18,7 @@ Workloads (all seeded, synthetic):
 """
 from __future__ import annotations
 
+import functools
 import random
 from dataclasses import dataclass, field
 from typing import List
@@ -72,22 +73,37 @@ def normalize(v: int) -> int:
     return v
 
 
+_REV8 = bytes(int(f"{b:08b}"[::-1], 2) for b in range(256))
+_M64 = (1 << 64) - 1
+
+
+def _transpose8(x: int) -> int:
+    """(r, c) -> (c, r) on an 8x8 bitboard (bit 8r + c): three delta swaps
+    (the classic diagonal flip of chess bitboards)."""
+    t = 0x0F0F0F0F00000000 & (x ^ (x << 28))
+    x ^= t ^ (t >> 28)
+    t = 0x3333000033330000 & (x ^ (x << 14))
+    x ^= t ^ (t >> 14)
+    t = 0x5500550055005500 & (x ^ (x << 7))
+    x ^= t ^ (t >> 7)
+    return x & _M64
+
+
 def transform(v: int, t: int) -> int:
-    sw, fx, fy = (t >> 2) & 1, t & 1, (t >> 1) & 1
-    out = 0
-    for b in range(64):
-        if (v >> b) & 1:
-            r, c = divmod(b, 8)
-            if fy:
-                r = 7 - r
-            if fx:
-                c = 7 - c
-            if sw:
-                r, c = c, r
-            out |= 1 << (8 * r + c)
+    """Transform t of the reference's order: bit 1 flips rows (r -> 7 - r),
+    bit 0 flips columns (c -> 7 - c), then bit 2 swaps rows and columns."""
+    b = v.to_bytes(8, "little")
+    if (t >> 1) & 1:
+        b = b[::-1]
+    if t & 1:
+        b = b.translate(_REV8)
+    out = int.from_bytes(b, "little")
+    if (t >> 2) & 1:
+        out = _transpose8(out)
     return normalize(out)
 
 
+@functools.lru_cache(maxsize=1 << 16)
 def canonical(v: int, forms: int = FULL_D4) -> int:
     return min(transform(v, t) for t in range(8) if (forms >> t) & 1)
 

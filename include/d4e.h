@@ -169,6 +169,10 @@ typedef struct d4e_stats {
     uint64_t splits;            /* batch groups split after a table overflow */
     uint64_t failed;            /* instances that ended with an error */
     uint64_t restarts;          /* solve-one attempts redone with a wider sample */
+    double step_wall_ms;        /* host wall time inside the engine's row steps */
+    double upload_ms;           /* ... of which: uploading new instances */
+    double keep_ms;             /* ... keeping solve-one levels */
+    double trace_ms;            /* ... tracing solve-one tilings */
 } d4e_stats;
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st);
@@ -260,14 +264,19 @@ int d4e_batch_run(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *o
  * projected device bytes of the admitted requests (frontier + hash table of
  * their next row) stay within memory_budget; admitted requests join the
  * running batch at its next row, so work of requests that arrived at
- * different times shares each k_expand / k_compact launch.  Results are the
- * same as alone (counts exact; solve-one tilings as in d4e_batch_run).
+ * different times shares each k_expand / k_compact launch.  Two lanes run
+ * concurrently on their own streams: every request starts in the fast lane
+ * (rows of at most 2^17 distinct states); one that outgrows it restarts in
+ * the slow lane, whose kernels leave room on every SM for the fast lane's.
+ * Results are the same as alone (counts exact; solve-one tilings as in
+ * d4e_batch_run).
  * ---------------------------------------------------------------------- */
 typedef struct d4e_server d4e_server;
 
 typedef struct d4e_server_opts {
     int32_t device;
-    uint32_t max_active;        /* requests on the device at once (0 = 8192) */
+    uint32_t max_active;        /* fast-lane requests on the device at once (0 = 4096);
+                                   the slow lane takes max_active / 16 (at least 16) */
     uint64_t memory_budget;     /* admission budget in bytes (0 = 150 GB, capped at the
                                    device's memory less 10%) */
     uint64_t max_states;        /* per-request limit on one row's frontier (0 = none) */
@@ -293,7 +302,14 @@ typedef struct d4e_server_stats {
     uint64_t peak_active;       /* most requests on the device at once */
     uint64_t peak_projected;    /* largest projected bytes admitted */
     uint64_t states_out;        /* distinct states produced (all requests) */
-    double busy_ms;             /* worker time spent in device steps */
+    double busy_ms;             /* worker time spent in device steps (both lanes) */
+    uint64_t moved;             /* requests restarted in the slow lane */
+    uint64_t lane_steps[2];     /* per lane (fast, slow): engine steps */
+    double lane_busy_ms[2];     /* per lane: wall time in engine steps */
+    double lane_kernel_ms[2];   /* per lane: k_expand + k_compact device time */
+    uint64_t lane_inst_rows[2]; /* per lane: instance-rows advanced */
+    uint64_t restarts;          /* solve-one attempts redone with a wider sample */
+    uint64_t paused;            /* instance-rows that waited for memory */
 } d4e_server_stats;
 
 int d4e_server_stats_get(d4e_server *s, d4e_server_stats *st);

@@ -18,7 +18,7 @@ def E(engine):
 def mix_requests(n, seed):
     from d4gb.problem import batched_mix
 
-    probs = [p for p in batched_mix(seed, 6 * n) if p.cells <= 56][:n]
+    probs = [p for p in batched_mix(seed, 6 * n) if p.cells <= 64][:n]
     modes = [1 if (i * 7) % 10 < 7 else 0 for i in range(len(probs))]   # 70% solve-one
     return probs, modes
 
@@ -63,6 +63,7 @@ def test_server_results_equal_alone(E, oracle):
             assert oracle.check_tiling(p, types, masks)
     assert st["completed"] == len(probs)
     assert st["peak_active"] > 1     # requests overlapped on the device
+    assert st["moved"] > 0           # some outgrew the fast lane and restarted
     assert all(got[i]["latency_ms"] >= got[i]["queued_ms"] >= 0 for i in got)
 
 
