@@ -67,6 +67,8 @@ def parse_args():
     ap.add_argument("--cpu-budget", type=float, default=15.0,
                     help="seconds of host CPU work for the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the launch autotuner (it runs in the first warm-up step)")
     return ap.parse_args()
 
 
@@ -209,10 +211,10 @@ def profiled_traffic() -> dict | None:
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
-def run_once(E, prob, device: int) -> dict:
+def run_once(E, prob, device: int, autotune: bool = True) -> dict:
     t0 = time.perf_counter()
     f = E.Frow(prob.shapes, prob.counts, prob.sym, prob.width, device=device)
-    s = E.CudaSearcher(f, rows=prob.rows)
+    s = E.CudaSearcher(f, rows=prob.rows, autotune=autotune)
     s.run()
     count = s.count()
     wall = time.perf_counter() - t0
@@ -254,7 +256,7 @@ def bench_ours(args, dist: Dist) -> None:
     dev = dist.local_rank
     prob, workload = make_problem(args)
     for _ in range(args.warmup):
-        run_once(E, prob, dev)
+        run_once(E, prob, dev, not args.no_autotune)
     flush_l2(dev)
     dist.barrier()
     sampler = ClockSampler(dev)
@@ -262,7 +264,7 @@ def bench_ours(args, dist: Dist) -> None:
     runs = []
     t_start = time.perf_counter()
     for _ in range(args.steps):
-        runs.append(run_once(E, prob, dev))
+        runs.append(run_once(E, prob, dev, not args.no_autotune))
         flush_l2(dev)
     t_wall = time.perf_counter() - t_start
     clocks = sampler.stop()
@@ -319,6 +321,11 @@ def bench_ours(args, dist: Dist) -> None:
             "states_per_step": states // args.steps,
             "raw_children_per_step": sum(s["states_raw"] for s in st) // args.steps,
             "record_bytes": st[0]["record_bytes"],
+            "launch_plan": {"autotuned": not args.no_autotune,
+                            "chunk_cap": st[0]["tuned_chunk_cap"],
+                            "chunks_per_warp": st[0]["tuned_chunks_per_warp"],
+                            "ctas_per_sm": st[0]["tuned_ctas_per_sm"] or "occupancy",
+                            "table_load": st[0]["tuned_load"]},
             "slot_bytes": st[0]["slot_bytes"],
             "l2": "frontier and table far larger than L2 (GBs); plus a 512 MiB L2 flush between steps",
             "parallelism": f"replicas x{dist.world} (no sharding, no collectives)",

@@ -184,6 +184,7 @@ static int make_searcher(const d4e_frow *f, uint32_t height, const uint8_t *rows
     d4e::EngineOpts o;
     o.device = f->device;
     o.keep_levels = (flags & D4E_KEEP_LEVELS) != 0;
+    o.autotune = (flags & D4E_AUTOTUNE) != 0;
     s->eng = std::make_unique<d4e::Engine>(o);
     d4e::InstanceSpec sp;
     sp.width = f->width;
@@ -348,6 +349,12 @@ static void fill_stats(const d4e::Engine &e, d4e_stats *st, bool add = false) {
     st->upload_ms += t.upload_ms;
     st->keep_ms += t.keep_ms;
     st->trace_ms += t.trace_ms;
+    st->tune_ms += t.tune_ms;
+    const d4e::Tuning &tu = e.tuning();
+    st->tuned_chunk_cap = tu.chunk_cap;
+    st->tuned_chunks_per_warp = tu.chunks_per_warp;
+    st->tuned_ctas_per_sm = (uint64_t)std::max(tu.ctas_per_sm, 0);
+    st->tuned_load = tu.load;
 }
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st) {
@@ -466,6 +473,8 @@ void engine_result(Engine &eng, uint32_t id, uint32_t mode, d4e_result *r) {
 
 extern "C" {
 
+void d4e_autotune_clear(void) { d4e::autotune_clear(); }
+
 int d4e_batch_run(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
                   d4e_result *results, d4e_stats *st) {
     return guarded([&] {
@@ -492,6 +501,7 @@ int d4e_batch_run(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *o
         eo.isolate_failures = true;
         if (o.flags & D4E_BATCH_WIDE_KEYS)
             eo.key_mode = d4e::KeyMode::K128;
+        eo.autotune = (o.flags & D4E_BATCH_AUTOTUNE) != 0;
         if (st)
             std::memset(st, 0, sizeof(*st));
         if (o.flags & D4E_BATCH_SEQUENTIAL) {

@@ -3,6 +3,10 @@
 
 #include <algorithm>
 #include <chrono>
+#include <tuple>
+#include <mutex>
+#include <map>
+#include <functional>
 #include <cstring>
 
 #include "kernels.h"
@@ -95,6 +99,15 @@ uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
 // a third of the 129 MB L2, leaving the rest to the hash table's hot lines.
 constexpr uint64_t kGroupTableBytes = 48ull << 20;
 
+// Rows the autotuner measures on: big enough to fill the GPU, small enough
+// that a dozen trial runs cost little.
+constexpr uint64_t kTuneMinStates = 1ull << 21;
+constexpr uint64_t kTuneMaxStates = 1ull << 25;
+
+// A candidate plan replaces the current one only when it is this much
+// faster (trial timings vary by a few percent).
+constexpr double kTuneGain = 0.97;
+
 uint32_t bit_length(uint64_t v) {
     uint32_t b = 0;
     while (v) {
@@ -137,6 +150,9 @@ Engine::Engine(const EngineOpts &opts) : opts_(opts) {
     nraw_.reserve(2, stream_);
     if (opts_.chunk_states < 32)
         opts_.chunk_states = 32;
+    tune_.chunk_cap = opts_.chunk_states;
+    tune_.load = opts_.target_load;
+    tune_.ctas_per_sm = opts_.expand_ctas_per_sm;
     if (opts_.k64_inst_bits) {
         if (opts_.k64_inst_bits > 23 || opts_.keep_levels)
             throw Error(kErrInvalid, "k64_inst_bits must be 1..23 (and no keep_levels)");
@@ -416,7 +432,7 @@ uint64_t Engine::projected_bytes(uint32_t id) const {
     const Inst &in = inst_.at(id);
     if (in.done)
         return 0;
-    const double per_state = (k64_ ? 16.0 : 24.0) + (double)(slot_units() * 16) / opts_.target_load;
+    const double per_state = (k64_ ? 16.0 : 24.0) + (double)(slot_units() * 16) / tune_.load;
     const double est = (double)std::max<uint64_t>(in.seg_len, 1) * in.growth;
     return (uint64_t)(est * per_state + (double)in.seg_len * (k64_ ? 16.0 : 24.0));
 }
@@ -426,7 +442,7 @@ uint64_t Engine::peak_bytes(uint32_t id) const {
     uint64_t peak = 1;
     for (uint64_t v : in.level_sizes)
         peak = std::max(peak, v);
-    const double per_state = (k64_ ? 16.0 : 24.0) + (double)(slot_units() * 16) / opts_.target_load;
+    const double per_state = (k64_ ? 16.0 : 24.0) + (double)(slot_units() * 16) / tune_.load;
     return (uint64_t)((double)peak * per_state);
 }
 
@@ -487,7 +503,7 @@ uint64_t Engine::table_capacity(uint64_t want) {
     const double avail = memory_limit((double)table_.cap * sizeof(ulonglong2) + (double)free_b -
                                       0.1 * (double)total_b);
     const uint64_t limit =
-        avail > 0 ? (uint64_t)(avail / ((double)slot_bytes + opts_.target_load * rec_bytes)) : 0;
+        avail > 0 ? (uint64_t)(avail / ((double)slot_bytes + tune_.load * rec_bytes)) : 0;
     return std::max<uint64_t>(std::min<uint64_t>(want, limit / 1024 * 1024), 1ull << 20);
 }
 
@@ -619,7 +635,7 @@ StepStats Engine::step_impl() {
     for (uint32_t id : order) {
         const Inst &in = inst_[id];
         const double est = (double)std::max<uint64_t>(in.seg_len, 1) * in.growth;
-        const double f = est * rec_bytes, t = est / opts_.target_load * (double)slot_bytes;
+        const double f = est * rec_bytes, t = est / tune_.load * (double)slot_bytes;
         const double seg_b = (double)in.seg_len * rec_bytes;
         const double need = run_front + f + (paused_bytes - seg_b) + std::max(run_table, t);
         if (run.empty() || need <= mem) {
@@ -652,7 +668,7 @@ StepStats Engine::step_impl() {
         for (uint32_t id : run) {
             const Inst &in = inst_[id];
             const double e = (double)std::max<uint64_t>(in.seg_len, 1) * in.growth /
-                             opts_.target_load;
+                             tune_.load;
             const double tab = (double)(in.lib.plc.size() * sizeof(Plc) +
                                         in.lib.filters.size() * sizeof(unsigned long long) +
                                         sizeof(InstDesc));
@@ -699,31 +715,42 @@ StepStats Engine::step_impl() {
             fan = 0;
         const uint64_t per = fan ? fan : 1;
         const uint64_t items = n_grp * per;
-        // Warps take chunks independently: about eight chunks per resident
-        // warp, within [32, chunk_states] items.
-        const uint64_t warps = slots * 8;
-        uint64_t chunk = (items + 8 * warps - 1) / (8 * warps);
-        chunk = std::min<uint64_t>(std::max<uint64_t>(round_up(chunk, 32), 32),
-                                   opts_.chunk_states);
+        // Launch plan: warps take chunks independently, about
+        // `chunks_per_warp` chunks per resident warp, within [32, chunk_cap]
+        // items; the grid is `ctas` CTAs per SM.
         std::vector<Seg> segs;
-        segs.reserve(grp.size());
-        uint64_t n_chunks = 0;
-        for (uint32_t id : grp) {
-            const Inst &in = inst_[id];
-            Seg s = seg_for(id, in.row);
-            s.begin = in.seg_begin * per;
-            s.len = in.seg_len * per;
-            s.chunk_base = n_chunks;
-            n_chunks += (s.len + chunk - 1) / chunk;
-            segs.push_back(s);
-        }
-        segs_.reserve(segs.size(), stream_);
-        cuda_check(cudaMemcpyAsync(segs_.p, segs.data(), segs.size() * sizeof(Seg),
-                                   cudaMemcpyHostToDevice, stream_),
-                   "upload segments");
-        tot_.h2d_bytes += segs.size() * sizeof(Seg);
+        uint64_t chunk = 0, n_chunks = 0;
+        int grid = 0;
+        auto plan = [&](const Tuning &t) {
+            const int ctas = t.ctas_per_sm > 0 ? std::min(t.ctas_per_sm, occ) : occ;
+            const uint64_t warps = (uint64_t)sms_ * (uint64_t)ctas * 8;
+            const uint64_t cpw = t.chunks_per_warp;
+            chunk = (items + cpw * warps - 1) / (cpw * warps);
+            chunk = std::min<uint64_t>(std::max<uint64_t>(round_up(chunk, 32), 32), t.chunk_cap);
+            segs.clear();
+            n_chunks = 0;
+            for (uint32_t id : grp) {
+                const Inst &in = inst_[id];
+                Seg s = seg_for(id, in.row);
+                s.begin = in.seg_begin * per;
+                s.len = in.seg_len * per;
+                s.chunk_base = n_chunks;
+                n_chunks += (s.len + chunk - 1) / chunk;
+                segs.push_back(s);
+            }
+            segs_.reserve(segs.size(), stream_);
+            cuda_check(cudaMemcpyAsync(segs_.p, segs.data(), segs.size() * sizeof(Seg),
+                                       cudaMemcpyHostToDevice, stream_),
+                       "upload segments");
+            tot_.h2d_bytes += segs.size() * sizeof(Seg);
+            grid = (int)std::min<uint64_t>(n_chunks, (uint64_t)sms_ * (uint64_t)ctas);
+        };
+        if (opts_.autotune && !tune_.set && !fan && n_grp >= kTuneMinStates &&
+            n_grp <= kTuneMaxStates)
+            autotune(grp, est, occ, plan, segs, chunk, n_chunks, grid);
+        plan(tune_);
 
-        uint64_t cap = table_capacity((uint64_t)(std::max(est, 1.0) / opts_.target_load));
+        uint64_t cap = table_capacity((uint64_t)(std::max(est, 1.0) / tune_.load));
         unsigned int h_status = 0;
         unsigned long long h_raw = 0;
         bool split = false;
@@ -763,7 +790,6 @@ StepStats Engine::step_impl() {
             a.status = misc_.p;
             a.work = nraw_.p + 1;
             a.max_probe = opts_.max_probe;
-            const int grid = (int)std::min<uint64_t>(n_chunks, slots);
             cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
             launch_expand(k64_, a, grid, stream_);
             cuda_check(cudaGetLastError(), "k_expand launch");
@@ -796,7 +822,7 @@ StepStats Engine::step_impl() {
             st.retries++;
             tot_.retries++;
             const uint64_t want =
-                std::max<uint64_t>(cap * 4, (uint64_t)((double)h_raw / opts_.target_load));
+                std::max<uint64_t>(cap * 4, (uint64_t)((double)h_raw / tune_.load));
             const uint64_t grown = table_capacity(want);
             if (grown >= want || (grp.size() == 1 && grown > cap)) {
                 cap = grown;
@@ -1080,6 +1106,156 @@ StepStats Engine::step_impl() {
     tot_.peak_frontier = std::max<uint64_t>(tot_.peak_frontier, st.n_out);
     tot_.paused += st.paused;
     return st;
+}
+
+namespace {
+
+// Tuned launch parameters per (key encoding, board width, device), shared
+// by every engine of the process.
+struct TuneKey {
+    bool k64;
+    uint32_t width;
+    int device;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(k64, width, device) < std::tie(o.k64, o.width, o.device);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, Tuning> g_tune_cache;
+
+}  // namespace
+
+void autotune_clear() {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache.clear();
+}
+
+void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
+                      const std::function<void(const Tuning &)> &plan,
+                      const std::vector<Seg> &segs, const uint64_t &chunk,
+                      const uint64_t &n_chunks, const int &grid) {
+    // Replaces the reference's launch-sizing model (KSizing::optimize /
+    // KParams::fom, src/kernel.cu:99-236) with measurement: the row about to
+    // run is expanded and compacted (children discarded) under candidate
+    // launch plans, and the fastest is kept -- first the CTAs per SM, then
+    // the chunk sizing, then the table load factor.
+    const TuneKey key{k64_, inst_[grp[0]].width, opts_.device};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            tune_ = it->second;
+            return;
+        }
+    }
+    const auto t0 = HostClock::now();
+    const size_t n_inst = inst_.size();
+    std::vector<unsigned long long> drop(n_inst, kCursorDrop);
+    cuda_check(cudaMemcpyAsync(cursor_.p, drop.data(), n_inst * sizeof(unsigned long long),
+                               cudaMemcpyHostToDevice, stream_),
+               "upload cursors");
+    auto trial = [&](const Tuning &t) -> double {
+        plan(t);
+        const uint64_t cap = table_capacity((uint64_t)(std::max(est, 1.0) / t.load));
+        const uint64_t units = cap * slot_units();
+        if (table_.cap < units) {
+            table_.release();
+            table_clean_ = 0;
+            table_.reserve(units, stream_);
+        }
+        if (table_clean_ < units) {
+            cuda_check(cudaMemsetAsync(table_.p + table_clean_, 0,
+                                       (units - table_clean_) * sizeof(ulonglong2), stream_),
+                       "memset table");
+            table_clean_ = units;
+        }
+        cuda_check(cudaMemsetAsync(inst_unique_.p, 0, n_inst * sizeof(unsigned int), stream_),
+                   "memset");
+        cuda_check(cudaMemsetAsync(misc_.p, 0, 4 * sizeof(unsigned int), stream_), "memset");
+        cuda_check(cudaMemsetAsync(nraw_.p, 0, 2 * sizeof(unsigned long long), stream_), "memset");
+        ExpandArgs a{};
+        a.segs = segs_.p;
+        a.n_segs = (uint32_t)segs.size();
+        a.n_chunks = n_chunks;
+        a.chunk_states = chunk;
+        a.fan = 0;
+        a.insts = insts_.p;
+        a.plc = plc_.p;
+        a.filt = filt_.p;
+        a.recs = keys_[cur_].p;
+        a.cnts = cnts_[cur_].p;
+        a.table = table_.p;
+        a.cap = cap;
+        a.inst_unique = inst_unique_.p;
+        a.n_raw = nraw_.p;
+        a.status = misc_.p;
+        a.work = nraw_.p + 1;
+        a.max_probe = opts_.max_probe;
+        CompactArgs c{};
+        c.table = table_.p;
+        c.cap = cap;
+        c.cursor = cursor_.p;   // every instance dropped: scan and clear only
+        c.out_recs = keys_[1 - cur_].p;
+        c.out_cnts = cnts_[1 - cur_].p;
+        c.results = results_.p;
+        c.final_states = final_states_.p;
+        c.inst_off = inst_off_;
+        c.inst_mask = inst_mask_;
+        c.keep_max = nullptr;
+        const int cgrid = (int)std::min<uint64_t>((cap + 255) / 256, (uint64_t)sms_ * 8);
+        cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
+        launch_expand(k64_, a, grid, stream_);
+        launch_compact(k64_, c, cgrid, stream_);
+        cuda_check(cudaGetLastError(), "autotune launch");
+        cuda_check(cudaEventRecord(ev_[1], stream_), "cudaEventRecord");
+        unsigned int stt = 0;
+        cuda_check(cudaMemcpyAsync(&stt, misc_.p, sizeof(stt), cudaMemcpyDeviceToHost, stream_),
+                   "read status");
+        cuda_check(cudaStreamSynchronize(stream_), "autotune trial");
+        tot_.other_launches += 2;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
+        return (stt & kStatusTableOverflow) ? 1e30 : (double)ms;
+    };
+    Tuning best = tune_;
+    best.ctas_per_sm = occ;
+    trial(best);                       // warm-up
+    double best_ms = trial(best);
+    auto consider = [&](Tuning t) {
+        const double ms = trial(t);
+        if (ms < best_ms * kTuneGain) {
+            best_ms = ms;
+            best = t;
+        }
+    };
+    for (int c = occ - 1; c >= std::max(1, occ - 2); c--) {
+        Tuning t = best;
+        t.ctas_per_sm = c;
+        consider(t);
+    }
+    const Tuning base = best;
+    for (uint32_t cpw : {4u, 16u}) {
+        Tuning t = base;
+        t.chunks_per_warp = cpw;
+        consider(t);
+    }
+    const Tuning base2 = best;
+    for (uint64_t cap : {256ull, 512ull, 2048ull}) {
+        Tuning t = base2;
+        t.chunk_cap = cap;
+        consider(t);
+    }
+    const Tuning base3 = best;
+    for (double load : {0.35, 0.7}) {
+        Tuning t = base3;
+        t.load = load;
+        consider(t);
+    }
+    best.set = true;
+    tune_ = best;
+    tot_.tune_ms += host_ms_since(t0);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = best;
 }
 
 void Engine::keep_levels_of(const std::vector<uint32_t> &ids) {

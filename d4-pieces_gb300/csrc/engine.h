@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -61,6 +62,9 @@ struct DevBuf {
     void reserve(size_t n, cudaStream_t s, size_t keep = 0);
 };
 
+// Forgets the process-wide cache of measured launch plans.
+void autotune_clear();
+
 // Device bytes an allocation can still get: free memory plus what the
 // device's stream-ordered pools hold in reserve.
 size_t device_available_bytes(int device, size_t *total);
@@ -89,6 +93,18 @@ struct EngineOpts {
     // on every SM for kernels of another engine running concurrently.
     int expand_ctas_per_sm = 0;
     bool high_priority = false;    // create the engine's stream at the highest priority
+    // Measure launch plans on the first row of 2^21..2^25 states and keep
+    // the fastest (cached per key encoding, board width and device).
+    bool autotune = false;
+};
+
+// Launch plan of k_expand / k_compact and the table's load factor.
+struct Tuning {
+    bool set = false;                // measured (or taken from the cache)
+    uint64_t chunk_cap = 1024;       // most work items a warp takes at once
+    uint32_t chunks_per_warp = 8;    // chunks per resident warp aimed at
+    int ctas_per_sm = 0;             // k_expand CTAs per SM (0 = occupancy)
+    double load = 0.5;               // hash table load factor aimed at
 };
 
 enum class Mode : uint32_t { Count = 0, SolveOne = 1 };
@@ -129,6 +145,7 @@ struct Totals {
     // instances, keeping solve-one levels and tracing solve-one tilings
     // (each including the device work it waits for).
     double step_wall_ms = 0.0, upload_ms = 0.0, keep_ms = 0.0, trace_ms = 0.0;
+    double tune_ms = 0.0;          // host wall time spent in autotuning trials
 };
 
 // One kept frontier level of a solve-one instance: `len` records from
@@ -188,6 +205,7 @@ public:
                        bool single);
 
     const Totals &totals() const { return tot_; }
+    const Tuning &tuning() const { return tune_; }
     void set_max_frontier(uint64_t n) { opts_.max_frontier = n; }
     bool packed_keys() const { return k64_; }
     cudaStream_t stream() const { return stream_; }
@@ -220,6 +238,9 @@ private:
     };
 
     StepStats step_impl();
+    void autotune(const std::vector<uint32_t> &grp, double est, int occ,
+                  const std::function<void(const Tuning &)> &plan, const std::vector<Seg> &segs,
+                  const uint64_t &chunk, const uint64_t &n_chunks, const int &grid);
     void ensure_inst_capacity(size_t n);
     void fail_instance(uint32_t id, int code, const std::string &msg);
     // Solve-one support: kept levels, tracing, restarts with a wider sample.
@@ -307,6 +328,7 @@ private:
     DevBuf<TraceChain> chain_;
     DevBuf<TraceSeg> tsegs_;
 
+    Tuning tune_;
     Totals tot_;
     bool run_started_ = false;
     std::vector<unsigned int> h_unique_;

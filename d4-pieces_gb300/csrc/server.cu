@@ -95,6 +95,7 @@ public:
             eo.isolate_failures = true;
             eo.memory_budget = budget_;
             eo.high_priority = l == 0;
+            eo.autotune = true;
             if (l == 1 && occ > 1)
                 eo.expand_ctas_per_sm = occ - 1;
             EngineOpts e64 = eo;

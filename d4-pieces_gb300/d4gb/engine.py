@@ -29,6 +29,7 @@ D4E_ERR_NOMEM = -3
 D4E_ERR_UNSUPPORTED = -4
 D4E_ERR_STATE = -5
 D4E_KEEP_LEVELS = 1
+D4E_AUTOTUNE = 2
 D4E_BATCH_SEQUENTIAL = 1
 
 _u64p = C.POINTER(C.c_uint64)
@@ -69,6 +70,11 @@ class Stats(C.Structure):
         ("upload_ms", C.c_double),
         ("keep_ms", C.c_double),
         ("trace_ms", C.c_double),
+        ("tune_ms", C.c_double),
+        ("tuned_chunk_cap", C.c_uint64),
+        ("tuned_chunks_per_warp", C.c_uint64),
+        ("tuned_ctas_per_sm", C.c_uint64),
+        ("tuned_load", C.c_double),
     ]
 
     def as_dict(self) -> dict:
@@ -201,6 +207,7 @@ _sig("d4e_server_poll", C.c_int, C.c_void_p, C.POINTER(Result), C.c_uint32, _u32
 _sig("d4e_server_drain", C.c_int, C.c_void_p, C.c_double)
 _sig("d4e_server_stats_get", C.c_int, C.c_void_p, C.POINTER(ServerStats))
 _sig("d4e_server_destroy", None, C.c_void_p)
+_sig("d4e_autotune_clear", None)
 _sig("d4e_canonical_grid", C.c_int, C.c_uint32, C.c_uint32, _u8p, _i8p, _i8p)
 _sig("d4e_count_noalloc", C.c_int, C.POINTER(Instance), C.c_void_p, _u64p, _u64p)
 
@@ -277,7 +284,8 @@ class CudaSearcher:
     """One puzzle, one board row per :meth:`search_GPU` (src/searcher_cuda.h:10-38)."""
 
     def __init__(self, frow: Frow, empty_area: Optional[int] = None,
-                 rows: Optional[Sequence[int]] = None, keep_levels: bool = False):
+                 rows: Optional[Sequence[int]] = None, keep_levels: bool = False,
+                 autotune: bool = False):
         self._frow = frow
         self._h = C.c_void_p()
         if empty_area is not None:
@@ -292,8 +300,8 @@ class CudaSearcher:
             self.rows = list(rows)
             self.width = frow.width
             r = _arr(C.c_uint8, self.rows)
-            _check(_lib.d4e_searcher_create_board(frow._h, len(self.rows), r,
-                                                  D4E_KEEP_LEVELS if keep_levels else 0,
+            flags = (D4E_KEEP_LEVELS if keep_levels else 0) | (D4E_AUTOTUNE if autotune else 0)
+            _check(_lib.d4e_searcher_create_board(frow._h, len(self.rows), r, flags,
                                                   C.byref(self._h)))
         self.height = len(self.rows)
 
@@ -388,23 +396,30 @@ MODE_SOLVE_ONE = 1
 
 
 D4E_BATCH_WIDE_KEYS = 2
+D4E_BATCH_AUTOTUNE = 4
 
 
 def batch_run(problems, mode: int = MODE_COUNT, sequential: bool = False, device: int = 0,
               memory_budget: int = 0, max_states: int = 0, beam: int = 0,
-              wide_keys: bool = False):
+              wide_keys: bool = False, autotune: bool = False):
     """Runs a batch through d4e_batch_run; returns (results, stats dict).
     Each result is a dict (status, count, found, rows, latency_ms, and for a
     found solve-one tiling height x width "grid" (types) and "steps")."""
     arr, keep = _instances(problems)
     n = len(problems)
     res = (Result * max(n, 1))()
-    flags = (D4E_BATCH_SEQUENTIAL if sequential else 0) | (D4E_BATCH_WIDE_KEYS if wide_keys else 0)
+    flags = ((D4E_BATCH_SEQUENTIAL if sequential else 0) | (D4E_BATCH_WIDE_KEYS if wide_keys else 0)
+             | (D4E_BATCH_AUTOTUNE if autotune else 0))
     o = BatchOpts(mode, flags, device, 0, memory_budget, max_states, beam)
     st = Stats()
     _check(_lib.d4e_batch_run(arr, n, C.byref(o), res, C.byref(st)))
     return ([res[i].as_dict(problems[i].width, problems[i].height) for i in range(n)],
             st.as_dict())
+
+
+def autotune_clear() -> None:
+    """Forgets the launch plans measured so far in this process."""
+    _lib.d4e_autotune_clear()
 
 
 class Server:

@@ -99,6 +99,12 @@ void d4e_frow_destroy(d4e_frow *f);
 typedef struct d4e_searcher d4e_searcher;
 
 #define D4E_KEEP_LEVELS 1u   /* retain every row's frontier: enables d4e_searcher_solutions */
+#define D4E_AUTOTUNE 2u      /* measure launch plans on the first row of 2^21..2^25 states
+                                (cached per process); replaces KSizing::optimize */
+
+/* Forgets every launch plan measured so far in this process (the next
+ * autotuned engine measures again). */
+void d4e_autotune_clear(void);
 
 /* CudaSearcher(uint64_t empty_area): 8-wide board, height = number of rows up
  * to the last cell to cover (src/searcher_cuda.cu:12-21).  The frow tables
@@ -106,7 +112,7 @@ typedef struct d4e_searcher d4e_searcher;
 int d4e_searcher_create(const d4e_frow *f, uint64_t empty_area, d4e_searcher **out);
 
 /* Board of any height 1..64 with the frow tables' width; flags = 0 or
- * D4E_KEEP_LEVELS. */
+ * D4E_KEEP_LEVELS | D4E_AUTOTUNE. */
 int d4e_searcher_create_board(const d4e_frow *f, uint32_t height, const uint8_t *rows,
                               uint32_t flags, d4e_searcher **out);
 
@@ -173,6 +179,11 @@ typedef struct d4e_stats {
     double upload_ms;           /* ... of which: uploading new instances */
     double keep_ms;             /* ... keeping solve-one levels */
     double trace_ms;            /* ... tracing solve-one tilings */
+    double tune_ms;             /* host time in autotuning trials */
+    uint64_t tuned_chunk_cap;   /* launch plan in use: most items a warp takes at once */
+    uint64_t tuned_chunks_per_warp; /* chunks per resident warp aimed at */
+    uint64_t tuned_ctas_per_sm; /* k_expand CTAs per SM (0 = occupancy) */
+    double tuned_load;          /* hash table load factor */
 } d4e_stats;
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st);
@@ -202,6 +213,7 @@ typedef struct d4e_instance {
 
 #define D4E_BATCH_SEQUENTIAL 1u /* one puzzle at a time, one launch sequence per puzzle */
 #define D4E_BATCH_WIDE_KEYS 2u  /* d4e_batch_run: the general 128-bit key encoding for all */
+#define D4E_BATCH_AUTOTUNE 4u   /* d4e_batch_run: measure launch plans (see D4E_AUTOTUNE) */
 
 /* Counts the tilings of every instance.  Default: all instances advance
  * together, one k_expand + one k_compact launch per board row for the whole
@@ -250,9 +262,9 @@ typedef struct d4e_result {
  * Solve-one: every row is de-duplicated as in counting; with beam > 0 a row
  * whose distinct states exceed beam keeps about beam of them, chosen by a
  * hash of the state alone.  When such an attempt dies out it is redone with
- * a 16x wider sample, and exactly from 2^24 states on, so "not found" is
- * always exact.  The tiling reported is the same whether the instance runs
- * alone or in any batch.  results[i].tag = i. */
+ * a 16x wider sample, and exactly once the sample width has passed 2^20
+ * states, so "not found" is always exact.  The tiling reported is the same
+ * whether the instance runs alone or in any batch.  results[i].tag = i. */
 int d4e_batch_run(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
                   d4e_result *results, d4e_stats *st);
 
