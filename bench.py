@@ -290,6 +290,12 @@ def bench_ours(args, dist: Dist) -> None:
     traffic_per_launch = None
     if traffic and traffic.get("workload") == workload:
         traffic_per_launch = traffic.get("dram_bytes_per_launch")
+    # Dedup output stage (k_compact): scans every table slot, writes each
+    # distinct state once and clears its slot.
+    cmp_ms = sum(s["compact_ms"] for s in st)
+    cmp_bytes = sum(s["compact_slots"] * s["slot_bytes"] + s["states_out"] * s["record_bytes"]
+                    + s["states_out"] * s["slot_bytes"] for s in st)
+    cmp_achieved = cmp_bytes / (cmp_ms / 1e3) / 1e9 if cmp_ms > 0 else None
     launches = sum(s["expand_launches"] + s["compact_launches"] + s["other_launches"] for s in st)
     h2d = sum(s["h2d_bytes"] for s in st) / len(st)
     d2h = sum(s["d2h_bytes"] for s in st) / len(st)
@@ -349,6 +355,16 @@ def bench_ours(args, dist: Dist) -> None:
             "algorithmic_bytes_per_launch": alg_bytes / exp_launches if exp_launches else None,
             "avg_launch_ms": exp_ms / exp_launches if exp_launches else None,
             "launches": exp_launches,
+        },
+        "dedup_roofline": {
+            "kernel": "k_compact (table scan -> distinct states, slots cleared)",
+            "bound": "hbm",
+            "achieved": cmp_achieved,
+            "peak": peaks["hbm_gbs"],
+            "unit": "GB/s",
+            "frac": cmp_achieved / peaks["hbm_gbs"] if cmp_achieved else None,
+            "bytes": "table slots scanned x slot bytes + distinct states x (record + slot) bytes",
+            "ms_per_step": cmp_ms / len(st),
         },
         "gpu_launches": launches,
         "clocks": clocks,

@@ -355,6 +355,7 @@ static void fill_stats(const d4e::Engine &e, d4e_stats *st, bool add = false) {
     st->tuned_chunks_per_warp = tu.chunks_per_warp;
     st->tuned_ctas_per_sm = (uint64_t)std::max(tu.ctas_per_sm, 0);
     st->tuned_load = tu.load;
+    st->compact_slots += t.compact_slots;
 }
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st) {

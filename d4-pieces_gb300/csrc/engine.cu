@@ -929,12 +929,13 @@ StepStats Engine::step_impl() {
         c.inst_off = inst_off_;
         c.inst_mask = inst_mask_;
         c.keep_max = sampled.empty() ? nullptr : keep_max_.p;
-        const int cgrid = (int)std::min<uint64_t>((cap + 255) / 256, (uint64_t)sms_ * 8);
+        const int cgrid = compact_grid(cap, sms_);
         cuda_check(cudaEventRecord(ev_[2], stream_), "cudaEventRecord");
         launch_compact(k64_, c, cgrid, stream_);
         cuda_check(cudaGetLastError(), "k_compact launch");
         cuda_check(cudaEventRecord(ev_[3], stream_), "cudaEventRecord");
         tot_.compact_launches++;
+        tot_.compact_slots += cap;
         cuda_check(cudaStreamSynchronize(stream_), "k_compact");
         float cms = 0.f;
         cudaEventElapsedTime(&cms, ev_[2], ev_[3]);
@@ -1202,7 +1203,7 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
         c.inst_off = inst_off_;
         c.inst_mask = inst_mask_;
         c.keep_max = nullptr;
-        const int cgrid = (int)std::min<uint64_t>((cap + 255) / 256, (uint64_t)sms_ * 8);
+        const int cgrid = compact_grid(cap, sms_);
         cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
         launch_expand(k64_, a, grid, stream_);
         launch_compact(k64_, c, cgrid, stream_);

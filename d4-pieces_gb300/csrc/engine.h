@@ -146,6 +146,7 @@ struct Totals {
     // (each including the device work it waits for).
     double step_wall_ms = 0.0, upload_ms = 0.0, keep_ms = 0.0, trace_ms = 0.0;
     double tune_ms = 0.0;          // host wall time spent in autotuning trials
+    uint64_t compact_slots = 0;    // table slots scanned by k_compact (sum over launches)
 };
 
 // One kept frontier level of a solve-one instance: `len` records from

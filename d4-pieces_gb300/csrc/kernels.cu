@@ -18,6 +18,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "state_hash.cuh"
 
 namespace d4e {
@@ -639,77 +641,205 @@ k_expand(ExpandArgs a) {
         atomicAdd(a.n_raw, tot);
 }
 
+// Compaction works on tiles of kCompactPer x 256 slots per block iteration
+// (slot tile_base + j * 256 + thread for round j).  When every occupied slot
+// of the tile belongs to one instance -- always for a single puzzle -- the
+// block computes output positions with ballots and one shared prefix and
+// reserves them with ONE cursor atomic per tile, writing coalesced runs.
+// Tiles holding several instances (batches) reserve per round and warp with
+// __match_any_sync aggregation instead.
+constexpr int kCompactPer = 8;
+constexpr int kCompactWarps = kCompactBlock / 32;
+
 template <bool K64>
 __global__ void __launch_bounds__(kCompactBlock)
 k_compact(CompactArgs a) {
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < a.cap;
-         base += stride) {
-        const unsigned long long i = base + threadIdx.x;
-        unsigned long long k0 = 0, k1 = 0, cnt = 0;
-        bool occ = false;
-        uint32_t inst = 0xFFFFFFFFu;
-        if (i < a.cap) {
-            if constexpr (K64) {
-                const ulonglong2 v = static_cast<const ulonglong2 *>(a.table)[i];
-                k0 = v.x;
-                cnt = v.y;
-                occ = k0 != 0ull;
-                if (occ)
-                    inst = (uint32_t)((k0 >> a.inst_off) & a.inst_mask);
-            } else {
-                const ulonglong4_32a v = static_cast<const ulonglong4_32a *>(a.table)[i];
-                k0 = v.x;
-                k1 = v.y;
-                cnt = v.z;
-                occ = k1 != 0ull;
-                if (occ)
-                    inst = (uint32_t)((k1 & ~kMarker) >> kInstShift128);
+    __shared__ unsigned int s_cnt[kCompactPer][kCompactWarps];   // stored slots per round, warp
+    __shared__ uint32_t s_min[kCompactWarps], s_max[kCompactWarps];
+    __shared__ unsigned long long s_base, s_fin_sum;
+    __shared__ unsigned int s_fin_n;
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned long long tile = (unsigned long long)kCompactPer * kCompactBlock;
+    for (unsigned long long tb = (unsigned long long)blockIdx.x * tile; tb < a.cap;
+         tb += (unsigned long long)gridDim.x * tile) {
+        unsigned long long k0[kCompactPer], k1[kCompactPer], cnt[kCompactPer];
+        uint32_t inst[kCompactPer];
+        uint32_t tmin = 0xFFFFFFFFu, tmax = 0u;
+#pragma unroll
+        for (int j = 0; j < kCompactPer; j++) {
+            const unsigned long long i = tb + (unsigned long long)j * kCompactBlock + threadIdx.x;
+            k0[j] = k1[j] = cnt[j] = 0;
+            inst[j] = 0xFFFFFFFFu;
+            if (i < a.cap) {
+                bool occ;
+                if constexpr (K64) {
+                    const ulonglong2 v = static_cast<const ulonglong2 *>(a.table)[i];
+                    k0[j] = v.x;
+                    cnt[j] = v.y;
+                    occ = v.x != 0ull;
+                    if (occ) {
+                        inst[j] = (uint32_t)((v.x >> a.inst_off) & a.inst_mask);
+                        static_cast<ulonglong2 *>(a.table)[i] = make_ulonglong2(0, 0);
+                    }
+                } else {
+                    const ulonglong4_32a v = static_cast<const ulonglong4_32a *>(a.table)[i];
+                    k0[j] = v.x;
+                    k1[j] = v.y;
+                    cnt[j] = v.z;
+                    occ = v.y != 0ull;
+                    if (occ) {
+                        inst[j] = (uint32_t)((v.y & ~kMarker) >> kInstShift128);
+                        static_cast<ulonglong4_32a *>(a.table)[i] =
+                            make_ulonglong4_32a(0, 0, 0, 0);
+                    }
+                }
+                if (occ) {
+                    tmin = min(tmin, inst[j]);
+                    tmax = max(tmax, inst[j]);
+                }
             }
         }
-        const unsigned long long cur = occ ? a.cursor[inst] : 0ull;
-        const bool fin = occ && cur == kCursorFinal;
-        bool store = occ && !fin && cur != kCursorDrop;
-        if (store && a.keep_max) {
-            // Sampled frontier: keep the states whose instance-free hash is
-            // below the instance's threshold.
-            const unsigned long long km = a.keep_max[inst];
-            if (km != ~0ull) {
-                unsigned long long wid;
-                if constexpr (K64)
-                    wid = k0 & ((1ull << a.inst_off) - 1ull);
-                else
-                    wid = witness128(k0, k1);
-                store = sample_hash(wid) <= km;
+        // Is the tile single-instance?
+        for (int o = 16; o > 0; o >>= 1) {
+            tmin = min(tmin, __shfl_xor_sync(0xffffffffu, tmin, o));
+            tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+        }
+        if (lane == 0) {
+            s_min[warp] = tmin;
+            s_max[warp] = tmax;
+        }
+        __syncthreads();
+        uint32_t bmin = 0xFFFFFFFFu, bmax = 0u;
+#pragma unroll
+        for (int w = 0; w < kCompactWarps; w++) {
+            bmin = min(bmin, s_min[w]);
+            bmax = max(bmax, s_max[w]);
+        }
+        if (bmin == 0xFFFFFFFFu) {   // empty tile
+            __syncthreads();
+            continue;
+        }
+        if (bmin == bmax) {
+            // ---- single instance: one reservation for the tile -------------
+            const uint32_t in0 = bmin;
+            const unsigned long long cur = a.cursor[in0];
+            const bool fin = cur == kCursorFinal;
+            const bool drop = cur == kCursorDrop;
+            const unsigned long long km = a.keep_max ? a.keep_max[in0] : ~0ull;
+            bool st[kCompactPer];
+            unsigned long long fsum = 0;
+            unsigned int fn = 0;
+#pragma unroll
+            for (int j = 0; j < kCompactPer; j++) {
+                const bool occ = inst[j] != 0xFFFFFFFFu;
+                st[j] = occ && !fin && !drop;
+                if (st[j] && km != ~0ull) {
+                    const unsigned long long wid =
+                        K64 ? (k0[j] & ((1ull << a.inst_off) - 1ull)) : witness128(k0[j], k1[j]);
+                    st[j] = sample_hash(wid) <= km;
+                }
+                if (occ && fin) {
+                    fsum += cnt[j];
+                    fn++;
+                }
+                const unsigned b = __ballot_sync(0xffffffffu, st[j]);
+                if (lane == 0)
+                    s_cnt[j][warp] = __popc(b);
+            }
+            if (fin) {
+                for (int o = 16; o > 0; o >>= 1) {
+                    fsum += __shfl_xor_sync(0xffffffffu, fsum, o);
+                    fn += __shfl_xor_sync(0xffffffffu, fn, o);
+                }
+                if (threadIdx.x == 0) {
+                    s_fin_sum = 0;
+                    s_fin_n = 0;
+                }
+            }
+            __syncthreads();
+            if (fin) {
+                if (lane == 0 && fn) {
+                    atomicAdd(&s_fin_sum, fsum);
+                    atomicAdd(&s_fin_n, fn);
+                }
+                __syncthreads();
+                if (threadIdx.x == 0 && s_fin_n) {
+                    atomicAdd(&a.results[in0], s_fin_sum);
+                    atomicAdd(&a.final_states[in0], s_fin_n);
+                }
+                __syncthreads();
+                continue;
+            }
+            if (threadIdx.x == 0) {
+                unsigned int total = 0;
+                for (int j = 0; j < kCompactPer; j++)
+                    for (int w = 0; w < kCompactWarps; w++)
+                        total += s_cnt[j][w];
+                s_base = total ? atomicAdd(&a.cursor[in0], (unsigned long long)total) : 0ull;
+            }
+            __syncthreads();
+            // Position = base + stored slots before (round j, warp, lane).
+            unsigned long long pos = s_base;
+#pragma unroll
+            for (int j = 0; j < kCompactPer; j++) {
+                unsigned int before = 0;
+                for (int w = 0; w < kCompactWarps; w++)
+                    before += w < (int)warp ? s_cnt[j][w] : 0u;
+                const unsigned b = __ballot_sync(0xffffffffu, st[j]);
+                if (st[j]) {
+                    const unsigned long long p = pos + before + __popc(b & lt);
+                    if constexpr (K64) {
+                        a.out_recs[p] = make_ulonglong2(k0[j], cnt[j]);
+                    } else {
+                        a.out_recs[p] = make_ulonglong2(k0[j], k1[j]);
+                        a.out_cnts[p] = cnt[j];
+                    }
+                }
+                unsigned int round_total = 0;
+                for (int w = 0; w < kCompactWarps; w++)
+                    round_total += s_cnt[j][w];
+                pos += round_total;
+            }
+            __syncthreads();
+            continue;
+        }
+        // ---- several instances: warp-aggregated reservation per round ------
+#pragma unroll
+        for (int j = 0; j < kCompactPer; j++) {
+            const bool occ = inst[j] != 0xFFFFFFFFu;
+            const unsigned long long cur = occ ? a.cursor[inst[j]] : 0ull;
+            const bool fin = occ && cur == kCursorFinal;
+            bool store = occ && !fin && cur != kCursorDrop;
+            if (store && a.keep_max) {
+                const unsigned long long km = a.keep_max[inst[j]];
+                if (km != ~0ull) {
+                    const unsigned long long wid =
+                        K64 ? (k0[j] & ((1ull << a.inst_off) - 1ull)) : witness128(k0[j], k1[j]);
+                    store = sample_hash(wid) <= km;
+                }
+            }
+            const unsigned peers = __match_any_sync(0xffffffffu, store ? inst[j] : 0xFFFFFFFFu);
+            if (store) {
+                const unsigned leader = __ffs(peers) - 1;
+                unsigned long long basepos = 0;
+                if (lane == leader)
+                    basepos = atomicAdd(&a.cursor[inst[j]], (unsigned long long)__popc(peers));
+                basepos = __shfl_sync(peers, basepos, leader);
+                const unsigned long long p = basepos + __popc(peers & lt);
+                if constexpr (K64) {
+                    a.out_recs[p] = make_ulonglong2(k0[j], cnt[j]);
+                } else {
+                    a.out_recs[p] = make_ulonglong2(k0[j], k1[j]);
+                    a.out_cnts[p] = cnt[j];
+                }
+            }
+            if (fin) {
+                atomicAdd(&a.results[inst[j]], cnt[j]);
+                atomicAdd(&a.final_states[inst[j]], 1u);
             }
         }
-        // Warp-aggregated cursor bump per instance.
-        const unsigned peers = __match_any_sync(0xffffffffu, store ? inst : 0xFFFFFFFFu);
-        if (store) {
-            const unsigned leader = __ffs(peers) - 1;
-            unsigned long long basepos = 0;
-            if (lane == leader)
-                basepos = atomicAdd(&a.cursor[inst], (unsigned long long)__popc(peers));
-            basepos = __shfl_sync(peers, basepos, leader);
-            const unsigned long long pos = basepos + __popc(peers & ((1u << lane) - 1u));
-            if constexpr (K64) {
-                a.out_recs[pos] = make_ulonglong2(k0, cnt);
-            } else {
-                a.out_recs[pos] = make_ulonglong2(k0, k1);
-                a.out_cnts[pos] = cnt;
-            }
-        }
-        if (fin) {
-            atomicAdd(&a.results[inst], cnt);
-            atomicAdd(&a.final_states[inst], 1u);
-        }
-        if (occ) {
-            if constexpr (K64)
-                static_cast<ulonglong2 *>(a.table)[i] = make_ulonglong2(0, 0);
-            else
-                static_cast<ulonglong4_32a *>(a.table)[i] = make_ulonglong4_32a(0, 0, 0, 0);
-        }
+        __syncthreads();
     }
 }
 
@@ -860,6 +990,13 @@ void launch_expand(bool k64, const ExpandArgs &a, int grid, cudaStream_t s) {
         k_expand<true><<<grid, kExpandBlock, 0, s>>>(a);
     else
         k_expand<false><<<grid, kExpandBlock, 0, s>>>(a);
+}
+
+int compact_grid(unsigned long long cap, int sms) {
+    const unsigned long long tile = (unsigned long long)kCompactPer * kCompactBlock;
+    const unsigned long long tiles = (cap + tile - 1) / tile;
+    return (int)std::max<unsigned long long>(1ull, std::min<unsigned long long>(tiles,
+                                                                              (unsigned long long)sms * 8));
 }
 
 void launch_compact(bool k64, const CompactArgs &a, int grid, cudaStream_t s) {

@@ -60,6 +60,10 @@ void launch_expand(bool k64, const ExpandArgs &a, int grid, cudaStream_t s);
 // the table.
 void launch_compact(bool k64, const CompactArgs &a, int grid, cudaStream_t s);
 
+// k_compact grid for a table of `cap` slots (tiles of 2048 slots, at most
+// 8 blocks per SM).
+int compact_grid(unsigned long long cap, int sms);
+
 // Solution reconstruction -------------------------------------------------
 struct KeySetArgs {
     void *table;

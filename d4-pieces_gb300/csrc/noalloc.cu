@@ -277,9 +277,7 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
             c.final_states = d_final;
             c.inst_off = lib.dyn_bits + lib.used_bits;
             c.inst_mask = 0;
-            launch_compact(k64, c, (int)std::min<uint64_t>((L.cap_slots + 255) / 256,
-                                                           (uint64_t)sms * 8),
-                           s);
+            launch_compact(k64, c, compact_grid(L.cap_slots, sms), s);
             cuda_check(cudaGetLastError(), "k_compact launch");
             if (last) {
                 cuda_check(cudaMemcpyAsync(&result, d_result, sizeof(result),

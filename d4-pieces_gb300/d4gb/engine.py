@@ -75,6 +75,7 @@ class Stats(C.Structure):
         ("tuned_chunks_per_warp", C.c_uint64),
         ("tuned_ctas_per_sm", C.c_uint64),
         ("tuned_load", C.c_double),
+        ("compact_slots", C.c_uint64),
     ]
 
     def as_dict(self) -> dict:

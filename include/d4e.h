@@ -184,6 +184,7 @@ typedef struct d4e_stats {
     uint64_t tuned_chunks_per_warp; /* chunks per resident warp aimed at */
     uint64_t tuned_ctas_per_sm; /* k_expand CTAs per SM (0 = occupancy) */
     double tuned_load;          /* hash table load factor */
+    uint64_t compact_slots;     /* hash-table slots scanned by k_compact (all launches) */
 } d4e_stats;
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st);
