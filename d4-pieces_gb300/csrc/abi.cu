@@ -356,6 +356,10 @@ static void fill_stats(const d4e::Engine &e, d4e_stats *st, bool add = false) {
     st->tuned_ctas_per_sm = (uint64_t)std::max(tu.ctas_per_sm, 0);
     st->tuned_load = tu.load;
     st->compact_slots += t.compact_slots;
+    const double ph[6] = {t.ph_select_ms, t.ph_table_ms, t.ph_expand_ms, t.ph_post_ms,
+                          t.ph_compact_ms, t.ph_tail_ms};
+    for (int i = 0; i < 6; i++)
+        st->phase_ms[i] += ph[i];
 }
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st) {

@@ -100,7 +100,17 @@ struct Seg {
     unsigned long long in_shift;  // K128: board row (row + R) entering window row R-1
     unsigned long long hi_board;  // K64: board rows [row + dyn_rows, row + R) in window coordinates
     unsigned long long tag;       // instance id bits | marker, in the mode's key coordinates
+    unsigned long long tbase;     // the instance's hash-table region: slots [tbase, tbase + tcap)
+    unsigned long long tcap;
 };
+
+// Per-instance new-key counter bit: the instance's table region overflowed
+// (its row is redone with a larger region; k_expand stops expanding it).
+constexpr uint32_t kUniqueOverflow = 0x80000000u;
+
+// Table regions are whole compaction tiles (2048 slots), so every tile k_compact
+// reads belongs to one instance.
+constexpr unsigned long long kRegionAlign = 2048;
 
 // Hash table slots.  A zero key is empty.
 struct alignas(32) Slot32 {

@@ -22,17 +22,28 @@ void cuda_check(cudaError_t e, const char *what) {
     }
 }
 
+namespace {
+thread_local cudaMemPool_t *tl_pool_ref = nullptr;
+}
+
+cudaError_t engine_malloc_async(void **p, size_t bytes, cudaStream_t s) {
+    if (tl_pool_ref && *tl_pool_ref)
+        return cudaMallocFromPoolAsync(p, bytes, *tl_pool_ref, s);
+    return cudaMallocAsync(p, bytes, s);
+}
+
 template <class T>
 void DevBuf<T>::reserve(size_t n, cudaStream_t stream, size_t keep) {
     if (n <= cap)
         return;
     size_t nc = std::max(n, cap + cap / 2);
     T *np = nullptr;
-    if (cudaMallocAsync(reinterpret_cast<void **>(&np), nc * sizeof(T), stream) != cudaSuccess) {
+    if (engine_malloc_async(reinterpret_cast<void **>(&np), nc * sizeof(T), stream) !=
+        cudaSuccess) {
         // Geometric growth did not fit: take exactly what is needed.
         cudaGetLastError();
         nc = n;
-        cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&np), nc * sizeof(T), stream),
+        cuda_check(engine_malloc_async(reinterpret_cast<void **>(&np), nc * sizeof(T), stream),
                    "cudaMallocAsync");
     }
     if (p) {
@@ -50,7 +61,10 @@ size_t device_available_bytes(int device, size_t *total) {
     size_t free_b = 0, total_b = 0;
     cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
     cudaMemPool_t pool;
-    cuda_check(cudaDeviceGetDefaultMemPool(&pool, device), "cudaDeviceGetDefaultMemPool");
+    if (tl_pool_ref && *tl_pool_ref)
+        pool = *tl_pool_ref;
+    else
+        cuda_check(cudaDeviceGetDefaultMemPool(&pool, device), "cudaDeviceGetDefaultMemPool");
     uint64_t reserved = 0, used = 0;
     cuda_check(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved),
                "cudaMemPoolGetAttribute");
@@ -93,6 +107,19 @@ struct DeviceGuard {
     }
 };
 
+// Memory pool of the engine whose method runs on this thread: engine
+// buffers come from the engine's own stream-ordered pool, so that engines on
+// other streams (the serving lanes) never wait on each other's frees.
+// Device + pool of one engine method call.
+struct EngineScope {
+    DeviceGuard dev;
+    cudaMemPool_t *prev;
+    EngineScope(int device, cudaMemPool_t *pool) : dev(device), prev(tl_pool_ref) {
+        tl_pool_ref = pool;
+    }
+    ~EngineScope() { tl_pool_ref = prev; }
+};
+
 uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
 
 // Placement + filter table bytes of one k_expand launch's instances: about
@@ -124,16 +151,19 @@ Engine::Engine(const EngineOpts &opts) : opts_(opts) {
     cuda_check(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
     if (opts_.device < 0 || opts_.device >= n)
         throw Error(kErrInvalid, "no such CUDA device");
-    DeviceGuard g(opts_.device);
+    EngineScope g(opts_.device, &pool_);
     cuda_check(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, opts_.device),
                "cudaDeviceGetAttribute");
     {
-        // Freed blocks stay in the device's default pool for the next
+        // The engine's own pool; freed blocks stay in it for the next
         // growth instead of going back to the driver at every sync.
-        cudaMemPool_t pool;
-        cuda_check(cudaDeviceGetDefaultMemPool(&pool, opts_.device), "cudaDeviceGetDefaultMemPool");
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = opts_.device;
+        cuda_check(cudaMemPoolCreate(&pool_, &props), "cudaMemPoolCreate");
         uint64_t keep_all = ~0ull;
-        cuda_check(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep_all),
+        cuda_check(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep_all),
                    "cudaMemPoolSetAttribute");
     }
     int prio_least = 0, prio_greatest = 0;
@@ -164,7 +194,7 @@ Engine::Engine(const EngineOpts &opts) : opts_(opts) {
 }
 
 Engine::~Engine() {
-    DeviceGuard g(opts_.device);
+    EngineScope g(opts_.device, &pool_);
     if (stream_)
         cudaStreamSynchronize(stream_);
     for (auto &c : chunks_) {
@@ -208,8 +238,12 @@ Engine::~Engine() {
         cnts_[i].release();
     }
     table_.release();
-    if (stream_)
+    if (stream_) {
+        cudaStreamSynchronize(stream_);
         cudaStreamDestroy(stream_);
+    }
+    if (pool_)
+        cudaMemPoolDestroy(pool_);
 }
 
 void Engine::ensure_inst_capacity(size_t n) {
@@ -224,7 +258,7 @@ void Engine::ensure_inst_capacity(size_t n) {
 }
 
 uint32_t Engine::add(const InstanceSpec &sp) {
-    DeviceGuard g(opts_.device);
+    EngineScope g(opts_.device, &pool_);
     if (sp.width < 1 || sp.width > (uint32_t)kMaxWidth)
         throw Error(kErrInvalid, "board width must be 1..8");
     if (sp.height < 1 || sp.height > (uint32_t)kMaxHeight)
@@ -487,24 +521,19 @@ ulonglong2 Engine::root_record(uint32_t id) const {
     return make_ulonglong2(in.root_window, kMarker | ((unsigned long long)id << kInstShift128));
 }
 
-uint64_t Engine::table_capacity(uint64_t want) {
-    // At least 1M slots (16-32 MB: cheap to clear, avoids regrowing on small
-    // rows), rounded to 1024; never more than the device can hold next to
-    // the next frontier (10% of the device kept back).
-    want = round_up(std::max<uint64_t>(want, 1ull << 20), 1024);
+uint64_t Engine::table_limit() {
+    // Most table slots the device (or the memory budget) can hold next to
+    // the current frontier, each paired with room for load * rec_bytes of
+    // next frontier, 10% of the device kept back; whole regions.
     const uint64_t slot_bytes = slot_units() * sizeof(ulonglong2);
-    if (want * slot_units() <= table_.cap)
-        return want;
     size_t total_b = 0;
     const size_t free_b = device_available_bytes(opts_.device, &total_b);
-    // Each slot is paired with room for load * rec_bytes of next frontier,
-    // so the bound does not depend on `want`.
     const double rec_bytes = k64_ ? 16.0 : 24.0;
     const double avail = memory_limit((double)table_.cap * sizeof(ulonglong2) + (double)free_b -
                                       0.1 * (double)total_b);
     const uint64_t limit =
         avail > 0 ? (uint64_t)(avail / ((double)slot_bytes + tune_.load * rec_bytes)) : 0;
-    return std::max<uint64_t>(std::min<uint64_t>(want, limit / 1024 * 1024), 1ull << 20);
+    return std::max<uint64_t>(limit / kRegionAlign * kRegionAlign, kRegionAlign);
 }
 
 int Engine::expand_occupancy() {
@@ -532,7 +561,7 @@ StepStats Engine::step() {
 }
 
 StepStats Engine::step_impl() {
-    DeviceGuard g(opts_.device);
+    EngineScope g(opts_.device, &pool_);
     StepStats st;
     fix_key_mode();
     if (tot_.steps == 0 && !run_started_) {
@@ -600,6 +629,12 @@ StepStats Engine::step_impl() {
     if (n_active_ == 0)
         return st;
 
+    auto t_phase = HostClock::now();
+    auto phase = [&](double &acc) {
+        const auto now = HostClock::now();
+        acc += std::chrono::duration<double, std::milli>(now - t_phase).count();
+        t_phase = now;
+    };
     // Active instances in frontier order.
     std::sort(active_.begin(), active_.end(),
               [&](uint32_t a, uint32_t b) { return inst_[a].seg_begin < inst_[b].seg_begin; });
@@ -692,6 +727,7 @@ StepStats Engine::step_impl() {
     // the largest table the device can hold is split in half and both halves
     // are redone.
     std::vector<std::vector<uint32_t>> work(groups.rbegin(), groups.rend());
+    phase(tot_.ph_select_ms);
     while (!work.empty()) {
         const std::vector<uint32_t> grp = std::move(work.back());
         work.pop_back();
@@ -718,10 +754,52 @@ StepStats Engine::step_impl() {
         // Launch plan: warps take chunks independently, about
         // `chunks_per_warp` chunks per resident warp, within [32, chunk_cap]
         // items; the grid is `ctas` CTAs per SM.
+        // Each instance inserts into its own table region, sized from its
+        // growth estimate at the plan's load and made of whole compaction
+        // tiles (so every k_compact tile belongs to one instance); at least
+        // 2^20 slots for the group.  total = 0: the group does not fit the
+        // memory the table may take and must be split.
+        const uint64_t limit = table_limit();
+        std::vector<uint64_t> region(grp.size());
+        auto layout = [&](double load) -> uint64_t {
+            uint64_t tot = 0;
+            for (size_t k = 0; k < grp.size(); k++) {
+                const Inst &in = inst_[grp[k]];
+                const double want =
+                    (double)std::max<uint64_t>(in.seg_len, 1) * in.growth / load;
+                // A first row's fan-out is unknown: at least 64K slots.
+                uint64_t r = std::max<uint64_t>((uint64_t)want, in.min_region);
+                if (in.row == 0)
+                    r = std::max<uint64_t>(r, 1ull << 16);
+                region[k] = round_up(std::max<uint64_t>(r, kRegionAlign), kRegionAlign);
+                tot += region[k];
+            }
+            if (tot < (1ull << 20)) {
+                const uint64_t scale = ((1ull << 20) + tot - 1) / tot;
+                tot = 0;
+                for (auto &r : region) {
+                    r *= scale;
+                    tot += r;
+                }
+            }
+            if (tot > limit) {
+                if (grp.size() > 1)
+                    return 0;
+                region[0] = limit / kRegionAlign * kRegionAlign;
+                tot = region[0];
+            }
+            return tot;
+        };
+        // Launch plan: warps take chunks independently, about
+        // `chunks_per_warp` chunks per resident warp, within [32, chunk_cap]
+        // items; the grid is `ctas` CTAs per SM.
         std::vector<Seg> segs;
         uint64_t chunk = 0, n_chunks = 0;
         int grid = 0;
-        auto plan = [&](const Tuning &t) {
+        auto plan = [&](const Tuning &t) -> uint64_t {
+            const uint64_t tot = layout(t.load);
+            if (!tot)
+                return 0;
             const int ctas = t.ctas_per_sm > 0 ? std::min(t.ctas_per_sm, occ) : occ;
             const uint64_t warps = (uint64_t)sms_ * (uint64_t)ctas * 8;
             const uint64_t cpw = t.chunks_per_warp;
@@ -729,12 +807,17 @@ StepStats Engine::step_impl() {
             chunk = std::min<uint64_t>(std::max<uint64_t>(round_up(chunk, 32), 32), t.chunk_cap);
             segs.clear();
             n_chunks = 0;
-            for (uint32_t id : grp) {
+            uint64_t tb = 0;
+            for (size_t k = 0; k < grp.size(); k++) {
+                const uint32_t id = grp[k];
                 const Inst &in = inst_[id];
                 Seg s = seg_for(id, in.row);
                 s.begin = in.seg_begin * per;
                 s.len = in.seg_len * per;
                 s.chunk_base = n_chunks;
+                s.tbase = tb;
+                s.tcap = region[k];
+                tb += region[k];
                 n_chunks += (s.len + chunk - 1) / chunk;
                 segs.push_back(s);
             }
@@ -744,117 +827,117 @@ StepStats Engine::step_impl() {
                        "upload segments");
             tot_.h2d_bytes += segs.size() * sizeof(Seg);
             grid = (int)std::min<uint64_t>(n_chunks, (uint64_t)sms_ * (uint64_t)ctas);
+            return tot;
         };
         if (opts_.autotune && !tune_.set && !fan && n_grp >= kTuneMinStates &&
             n_grp <= kTuneMaxStates)
             autotune(grp, est, occ, plan, segs, chunk, n_chunks, grid);
-        plan(tune_);
-
-        uint64_t cap = table_capacity((uint64_t)(std::max(est, 1.0) / tune_.load));
-        unsigned int h_status = 0;
+        const uint64_t cap = plan(tune_);
+        if (!cap) {
+            // The group's tables do not fit: split it.
+            const size_t half = grp.size() / 2;
+            work.emplace_back(grp.begin() + half, grp.end());
+            work.emplace_back(grp.begin(), grp.begin() + half);
+            tot_.splits++;
+            continue;
+        }
+        const uint64_t units = cap * slot_units();
+        if (table_.cap < units) {
+            table_.release();
+            table_clean_ = 0;
+            table_.reserve(units, stream_);
+        }
+        if (table_clean_ < units) {
+            cuda_check(cudaMemsetAsync(table_.p + table_clean_, 0,
+                                       (units - table_clean_) * sizeof(ulonglong2), stream_),
+                       "memset table");
+            table_clean_ = units;
+        }
+        cuda_check(cudaMemsetAsync(inst_unique_.p, 0, n_inst * sizeof(unsigned int), stream_),
+                   "memset");
+        cuda_check(cudaMemsetAsync(misc_.p, 0, 4 * sizeof(unsigned int), stream_), "memset");
+        cuda_check(cudaMemsetAsync(nraw_.p, 0, 2 * sizeof(unsigned long long), stream_), "memset");
+        phase(tot_.ph_table_ms);
+        ExpandArgs a;
+        a.segs = segs_.p;
+        a.n_segs = (uint32_t)segs.size();
+        a.n_chunks = n_chunks;
+        a.chunk_states = chunk;
+        a.fan = fan;
+        a.insts = insts_.p;
+        a.plc = plc_.p;
+        a.filt = filt_.p;
+        a.recs = keys_[cur_].p;
+        a.cnts = cnts_[cur_].p;
+        a.table = table_.p;
+        a.cap = cap;
+        a.inst_unique = inst_unique_.p;
+        a.n_raw = nraw_.p;
+        a.status = misc_.p;
+        a.work = nraw_.p + 1;
+        a.max_probe = opts_.max_probe;
+        cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
+        launch_expand(k64_, a, grid, stream_);
+        cuda_check(cudaGetLastError(), "k_expand launch");
+        cuda_check(cudaEventRecord(ev_[1], stream_), "cudaEventRecord");
+        tot_.expand_launches++;
         unsigned long long h_raw = 0;
-        bool split = false;
-        for (;;) {
-            const uint64_t units = cap * slot_units();
-            if (table_.cap < units) {
-                table_.release();
-                table_clean_ = 0;
-                table_.reserve(units, stream_);
-            }
-            if (table_clean_ < units) {
-                cuda_check(cudaMemsetAsync(table_.p + table_clean_, 0,
-                                           (units - table_clean_) * sizeof(ulonglong2), stream_),
-                           "memset table");
-                table_clean_ = units;
-            }
-            cuda_check(cudaMemsetAsync(inst_unique_.p, 0, n_inst * sizeof(unsigned int), stream_),
-                       "memset");
-            cuda_check(cudaMemsetAsync(misc_.p, 0, 4 * sizeof(unsigned int), stream_), "memset");
-            cuda_check(cudaMemsetAsync(nraw_.p, 0, 2 * sizeof(unsigned long long), stream_),
-                       "memset");
-            ExpandArgs a;
-            a.segs = segs_.p;
-            a.n_segs = (uint32_t)segs.size();
-            a.n_chunks = n_chunks;
-            a.chunk_states = chunk;
-            a.fan = fan;
-            a.insts = insts_.p;
-            a.plc = plc_.p;
-            a.filt = filt_.p;
-            a.recs = keys_[cur_].p;
-            a.cnts = cnts_[cur_].p;
-            a.table = table_.p;
-            a.cap = cap;
-            a.inst_unique = inst_unique_.p;
-            a.n_raw = nraw_.p;
-            a.status = misc_.p;
-            a.work = nraw_.p + 1;
-            a.max_probe = opts_.max_probe;
-            cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
-            launch_expand(k64_, a, grid, stream_);
-            cuda_check(cudaGetLastError(), "k_expand launch");
-            cuda_check(cudaEventRecord(ev_[1], stream_), "cudaEventRecord");
-            tot_.expand_launches++;
-            cuda_check(cudaMemcpyAsync(&h_status, misc_.p, sizeof(unsigned int),
-                                       cudaMemcpyDeviceToHost, stream_),
-                       "read status");
-            cuda_check(cudaMemcpyAsync(&h_raw, nraw_.p, sizeof(unsigned long long),
-                                       cudaMemcpyDeviceToHost, stream_),
-                       "read raw");
-            h_grp_unique_.resize(n_inst);
-            cuda_check(cudaMemcpyAsync(h_grp_unique_.data(), inst_unique_.p,
-                                       n_inst * sizeof(unsigned int), cudaMemcpyDeviceToHost,
-                                       stream_),
-                       "read unique");
-            cuda_check(cudaStreamSynchronize(stream_), "k_expand");
-            tot_.d2h_bytes += sizeof(unsigned int) + sizeof(unsigned long long) +
-                              n_inst * sizeof(unsigned int);
+        cuda_check(cudaMemcpyAsync(&h_raw, nraw_.p, sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, stream_),
+                   "read raw");
+        h_grp_unique_.resize(n_inst);
+        cuda_check(cudaMemcpyAsync(h_grp_unique_.data(), inst_unique_.p,
+                                   n_inst * sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_),
+                   "read unique");
+        cuda_check(cudaStreamSynchronize(stream_), "k_expand");
+        phase(tot_.ph_expand_ms);
+        tot_.d2h_bytes += sizeof(unsigned long long) + n_inst * sizeof(unsigned int);
+        {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
             st.expand_ms += ms;
-            if (!(h_status & kStatusTableOverflow))
-                break;
-            // Table too small for this group: clear it, then grow it (up to
-            // raw / load slots, which cannot overflow again) or, when the
-            // device cannot hold that, split the group.
-            cuda_check(cudaMemsetAsync(table_.p, 0, units * sizeof(ulonglong2), stream_),
-                       "memset table");
-            st.retries++;
-            tot_.retries++;
-            const uint64_t want =
-                std::max<uint64_t>(cap * 4, (uint64_t)((double)h_raw / tune_.load));
-            const uint64_t grown = table_capacity(want);
-            if (grown >= want || (grp.size() == 1 && grown > cap)) {
-                cap = grown;
-                continue;
-            }
-            if (grp.size() == 1) {
-                if (!opts_.isolate_failures)
-                    throw Error(kErrNoMem, "hash table cannot grow: device memory exhausted");
-                fail_instance(grp[0], kErrNoMem,
-                              "row does not fit the device: " + std::to_string(h_raw) +
-                                  " children");
-                st.failed++;
-            } else {
-                const size_t half = grp.size() / 2;
-                work.emplace_back(grp.begin() + half, grp.end());
-                work.emplace_back(grp.begin(), grp.begin() + half);
-                tot_.splits++;
-            }
-            split = true;
-            break;
         }
-        if (split)
-            continue;
         st.groups++;
-        // Only this group's counters are valid in the read-back.
-        for (uint32_t id : grp)
-            h_unique_[id] = h_grp_unique_[id];
         st.n_raw += h_raw;
         st.table_cap = std::max<uint64_t>(st.table_cap, cap);
+
+        // Instances whose region overflowed are redone, alone, with 4x the
+        // region (a lone instance at least raw / load); their partial
+        // children are dropped by this group's compaction.
+        std::vector<char> redo(grp.size(), 0);
+        std::vector<uint32_t> retry;
+        for (size_t k = 0; k < grp.size(); k++) {
+            const uint32_t id = grp[k];
+            if (!(h_grp_unique_[id] & kUniqueOverflow)) {
+                h_unique_[id] = h_grp_unique_[id];
+                continue;
+            }
+            redo[k] = 1;
+            h_unique_[id] = 0;
+            h_cursor_[id] = kCursorDrop;
+            st.retries++;
+            tot_.retries++;
+            Inst &in = inst_[id];
+            if (region[k] >= limit / kRegionAlign * kRegionAlign) {
+                if (!opts_.isolate_failures)
+                    throw Error(kErrNoMem, "hash table cannot grow: device memory exhausted");
+                fail_instance(id, kErrNoMem,
+                              "row does not fit the device: more than " +
+                                  std::to_string(region[k]) + " table slots");
+                st.failed++;
+                continue;
+            }
+            // Small regions grow fast (a wrong first guess costs a relaunch).
+            uint64_t grow = region[k] * (region[k] < (1ull << 18) ? 32 : 4);
+            if (grp.size() == 1)
+                grow = std::max<uint64_t>(grow, (uint64_t)((double)h_raw / tune_.load));
+            in.min_region = grow;
+            retry.push_back(id);
+        }
         uint64_t uniq = 0;
-        for (uint32_t id : grp)
-            uniq += h_unique_[id];
+        for (size_t k = 0; k < grp.size(); k++)
+            if (!redo[k])
+                uniq += h_unique_[grp[k]];
         if (opts_.max_frontier && st.n_out + uniq > opts_.max_frontier) {
             cuda_check(cudaMemsetAsync(table_.p, 0, cap * slot_units() * sizeof(ulonglong2),
                                        stream_),
@@ -866,7 +949,10 @@ StepStats Engine::step_impl() {
 
         // This group's next segments follow the previous groups' ones.
         const uint64_t off0 = off;
-        for (uint32_t id : grp) {
+        for (size_t k = 0; k < grp.size(); k++) {
+            const uint32_t id = grp[k];
+            if (redo[k])
+                continue;
             const Inst &in = inst_[id];
             const uint64_t u = h_unique_[id];
             if (in.limit && u > in.limit) {
@@ -899,10 +985,11 @@ StepStats Engine::step_impl() {
         // Solve-one instances over their sample width keep a hash-chosen
         // subset of about `beam` states (the same subset alone or batched).
         std::vector<uint32_t> sampled;
-        for (uint32_t id : grp) {
-            Inst &in = inst_[id];
-            if (in.mode == Mode::SolveOne && in.beam && !in.done && h_unique_[id] > in.beam)
-                sampled.push_back(id);
+        for (size_t k = 0; k < grp.size(); k++) {
+            Inst &in = inst_[grp[k]];
+            if (!redo[k] && in.mode == Mode::SolveOne && in.beam && !in.done &&
+                h_unique_[grp[k]] > in.beam)
+                sampled.push_back(grp[k]);
         }
         if (!sampled.empty()) {
             h_keep_max_.assign(n_inst, ~0ull);
@@ -930,6 +1017,7 @@ StepStats Engine::step_impl() {
         c.inst_mask = inst_mask_;
         c.keep_max = sampled.empty() ? nullptr : keep_max_.p;
         const int cgrid = compact_grid(cap, sms_);
+        phase(tot_.ph_post_ms);
         cuda_check(cudaEventRecord(ev_[2], stream_), "cudaEventRecord");
         launch_compact(k64_, c, cgrid, stream_);
         cuda_check(cudaGetLastError(), "k_compact launch");
@@ -937,9 +1025,18 @@ StepStats Engine::step_impl() {
         tot_.compact_launches++;
         tot_.compact_slots += cap;
         cuda_check(cudaStreamSynchronize(stream_), "k_compact");
+        phase(tot_.ph_compact_ms);
         float cms = 0.f;
         cudaEventElapsedTime(&cms, ev_[2], ev_[3]);
         st.compact_ms += cms;
+        // Table growth of the next row follows the distinct children the
+        // table had to hold (before sampling).
+        std::vector<double> table_growth(grp.size(), 0.0);
+        for (size_t k = 0; k < grp.size(); k++) {
+            const Inst &in = inst_[grp[k]];
+            if (in.seg_len)
+                table_growth[k] = (double)h_unique_[grp[k]] / (double)in.seg_len;
+        }
         if (!sampled.empty()) {
             // Kept states per sampled instance = cursor advance.
             std::vector<unsigned long long> cend(n_inst);
@@ -951,12 +1048,17 @@ StepStats Engine::step_impl() {
                 h_unique_[id] = (unsigned int)(cend[id] - h_cursor_[id]);
         }
         // Per-instance growth estimates for the next row.
-        for (uint32_t id : grp) {
-            Inst &in = inst_[id];
+        for (size_t k = 0; k < grp.size(); k++) {
+            Inst &in = inst_[grp[k]];
+            if (redo[k] || in.done)
+                continue;
+            in.min_region = 0;
             if (in.seg_len)
-                in.growth = std::clamp((double)h_unique_[id] / (double)in.seg_len * 1.25, 1.0,
-                                       256.0);
+                in.growth = std::clamp(table_growth[k] * 1.25, 1.0, 256.0);
         }
+        if (!retry.empty())
+            work.push_back(std::move(retry));
+        phase(tot_.ph_post_ms);
     }
     // Paused instances: their states move unchanged to the next frontier.
     std::vector<std::pair<uint32_t, uint64_t>> moved;   // (id, new begin)
@@ -1098,6 +1200,7 @@ StepStats Engine::step_impl() {
     if (st.n_in)
         growth_ = std::clamp((double)st.n_out / (double)st.n_in * 1.25, 1.0, 256.0);
 
+    phase(tot_.ph_tail_ms);
     tot_.steps++;
     tot_.states_in += st.n_in;
     tot_.states_raw += st.n_raw;
@@ -1132,7 +1235,7 @@ void autotune_clear() {
 }
 
 void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
-                      const std::function<void(const Tuning &)> &plan,
+                      const std::function<uint64_t(const Tuning &)> &plan,
                       const std::vector<Seg> &segs, const uint64_t &chunk,
                       const uint64_t &n_chunks, const int &grid) {
     // Replaces the reference's launch-sizing model (KSizing::optimize /
@@ -1155,9 +1258,11 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
     cuda_check(cudaMemcpyAsync(cursor_.p, drop.data(), n_inst * sizeof(unsigned long long),
                                cudaMemcpyHostToDevice, stream_),
                "upload cursors");
+    (void)est;
     auto trial = [&](const Tuning &t) -> double {
-        plan(t);
-        const uint64_t cap = table_capacity((uint64_t)(std::max(est, 1.0) / t.load));
+        const uint64_t cap = plan(t);
+        if (!cap)
+            return 1e30;
         const uint64_t units = cap * slot_units();
         if (table_.cap < units) {
             table_.release();
@@ -1216,6 +1321,8 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
         tot_.other_launches += 2;
         float ms = 0.f;
         cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
+        for (uint32_t id : grp)
+            inst_[id].min_region = 0;
         return (stt & kStatusTableOverflow) ? 1e30 : (double)ms;
     };
     Tuning best = tune_;
@@ -1268,13 +1375,13 @@ void Engine::keep_levels_of(const std::vector<uint32_t> &ids) {
     if (ids.empty() || total == 0)
         return;
     LvlChunk ch;
-    cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&ch.keys), total * sizeof(ulonglong2),
-                               stream_),
+    cuda_check(engine_malloc_async(reinterpret_cast<void **>(&ch.keys),
+                                   total * sizeof(ulonglong2), stream_),
                "cudaMallocAsync");
     ch.bytes = total * sizeof(ulonglong2);
     if (!k64_) {
-        cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&ch.cnts),
-                                   total * sizeof(unsigned long long), stream_),
+        cuda_check(engine_malloc_async(reinterpret_cast<void **>(&ch.cnts),
+                                       total * sizeof(unsigned long long), stream_),
                    "cudaMallocAsync");
         ch.bytes += total * sizeof(unsigned long long);
     }
@@ -1493,7 +1600,7 @@ bool Engine::solution(uint32_t id, int8_t *type_grid, int16_t *step_grid) {
 }
 
 uint64_t Engine::bucket_count(uint32_t id, uint32_t pattern) {
-    DeviceGuard g(opts_.device);
+    EngineScope g(opts_.device, &pool_);
     const Inst &in = inst_.at(id);
     if (!in.active)
         return 0;
@@ -1515,7 +1622,7 @@ uint64_t Engine::bucket_count(uint32_t id, uint32_t pattern) {
 void Engine::sync_results() {
     if (unfetched_.empty())
         return;
-    DeviceGuard g(opts_.device);
+    EngineScope g(opts_.device, &pool_);
     const uint32_t lo = *std::min_element(unfetched_.begin(), unfetched_.end());
     const uint32_t hi = *std::max_element(unfetched_.begin(), unfetched_.end()) + 1;
     std::vector<unsigned long long> r(hi - lo);
@@ -1550,7 +1657,7 @@ uint64_t Engine::count(uint32_t id) {
 
 uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t *step_grids,
                            bool single) {
-    DeviceGuard g(opts_.device);
+    EngineScope g(opts_.device, &pool_);
     if (!opts_.keep_levels)
         throw Error(kErrState, "solutions need an engine created with keep_levels");
     Inst &in = inst_.at(id);

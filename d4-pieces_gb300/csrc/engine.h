@@ -40,7 +40,11 @@ enum ErrCode : int {
 
 void cuda_check(cudaError_t e, const char *what);
 
-// Grow-only device buffer, allocated stream-ordered (cudaMallocAsync /
+// Stream-ordered allocation from the memory pool of the engine whose method
+// is running on this thread (the device's default pool outside engines).
+cudaError_t engine_malloc_async(void **p, size_t bytes, cudaStream_t s);
+
+// Grow-only device buffer, allocated stream-ordered (engine_malloc_async /
 // cudaFreeAsync on the owner's stream) so that growing it never
 // synchronises the device: engines on other streams keep running.
 template <class T>
@@ -146,6 +150,12 @@ struct Totals {
     // (each including the device work it waits for).
     double step_wall_ms = 0.0, upload_ms = 0.0, keep_ms = 0.0, trace_ms = 0.0;
     double tune_ms = 0.0;          // host wall time spent in autotuning trials
+    // Host wall time of step() phases: selecting / grouping instances,
+    // preparing tables (layout, allocation, clears), waiting for k_expand
+    // (launch to read-back), per-group bookkeeping, waiting for k_compact,
+    // and the row's tail (carries, levels, advancing instances).
+    double ph_select_ms = 0.0, ph_table_ms = 0.0, ph_expand_ms = 0.0, ph_post_ms = 0.0,
+           ph_compact_ms = 0.0, ph_tail_ms = 0.0;
     uint64_t compact_slots = 0;    // table slots scanned by k_compact (sum over launches)
 };
 
@@ -224,6 +234,7 @@ private:
         std::vector<uint64_t> level_sizes;
         unsigned long long root_window = 0;
         double growth = 256.0;       // expected children per state on the next row
+        uint64_t min_region = 0;     // table slots at least (after a region overflow)
         Mode mode = Mode::Count;
         uint64_t limit = 0;          // per-row frontier limit (0 = none)
         int status = 0;              // 0 or the ErrCode it failed with
@@ -240,8 +251,9 @@ private:
 
     StepStats step_impl();
     void autotune(const std::vector<uint32_t> &grp, double est, int occ,
-                  const std::function<void(const Tuning &)> &plan, const std::vector<Seg> &segs,
-                  const uint64_t &chunk, const uint64_t &n_chunks, const int &grid);
+                  const std::function<uint64_t(const Tuning &)> &plan,
+                  const std::vector<Seg> &segs, const uint64_t &chunk, const uint64_t &n_chunks,
+                  const int &grid);
     void ensure_inst_capacity(size_t n);
     void fail_instance(uint32_t id, int code, const std::string &msg);
     // Solve-one support: kept levels, tracing, restarts with a wider sample.
@@ -255,7 +267,7 @@ private:
     void fix_key_mode();
     void flush_uploads();
     int expand_occupancy();
-    uint64_t table_capacity(uint64_t want);
+    uint64_t table_limit();
     size_t slot_units() const { return k64_ ? 1 : 2; }   // table slot size in 16-byte units
     Seg seg_for(uint32_t id, uint32_t row) const;
     ulonglong2 root_record(uint32_t id) const;
@@ -320,6 +332,7 @@ private:
     std::vector<LvlChunk> chunks_;
     std::vector<uint32_t> free_chunks_;
     uint64_t lvl_bytes_ = 0;
+    cudaMemPool_t pool_ = nullptr;   // the engine's stream-ordered memory pool
     DevBuf<CopyRange> ranges_;
     DevBuf<unsigned long long> keep_max_;
     std::vector<unsigned long long> h_keep_max_;

@@ -287,29 +287,35 @@ struct WarpStage {
     unsigned long long k0[kStage];
     unsigned long long k1[kStage];
     unsigned long long cnt[kStage];
-    uint32_t inst[kStage];
+    uint32_t seg[kStage];   // producing segment | witness flag (bit 31)
 };
 
-// Returns true (warp-uniform) once the table has overflowed anywhere: the
-// level is redone with a larger table, so the expansion stops at once.
+// Inserts staged children into their instances' table regions.  An insert
+// that reaches the probe limit marks its instance (kUniqueOverflow: the
+// instance's row is redone with a larger region) and the status word.
+// Returns, per lane, the instance id of the child it failed to insert
+// (0xFFFFFFFF when none), so that lanes walking that instance can stop.
 template <bool K64>
-__device__ __forceinline__ bool flush_children(const ExpandArgs &a, const WarpStage &ws, int base,
-                                               int n, unsigned lane) {
+__device__ __forceinline__ uint32_t flush_children(const ExpandArgs &a, const WarpStage &ws,
+                                                   int base, int n, unsigned lane) {
     // Lane i inserts child base + i: up to 32 independent inserts in flight.
     int r = 2;
     uint32_t inst = 0xFFFFFFFFu;
     if ((int)lane < n) {
         const int j = base + (int)lane;
-        const uint32_t si = ws.inst[j];
+        const uint32_t si = ws.seg[j];
         const bool wmax = (si >> 31) != 0u;   // solve-one instance: value = witness
-        inst = si & 0x7FFFFFFFu;
+        const Seg &s = a.segs[si & 0x7FFFFFFFu];
+        inst = s.inst;
         if constexpr (K64)
-            r = insert64(static_cast<Slot16 *>(a.table), a.cap, ws.k0[j], ws.cnt[j], a.max_probe,
-                         wmax);
+            r = insert64(static_cast<Slot16 *>(a.table) + s.tbase, s.tcap, ws.k0[j], ws.cnt[j],
+                         a.max_probe, wmax);
         else
-            r = insert128(static_cast<Slot32 *>(a.table), a.cap, ws.k0[j], ws.k1[j], ws.cnt[j],
-                          a.max_probe, wmax);
+            r = insert128(static_cast<Slot32 *>(a.table) + s.tbase, s.tcap, ws.k0[j], ws.k1[j],
+                          ws.cnt[j], a.max_probe, wmax);
     }
+    if (r < 0)
+        atomicOr(&a.inst_unique[inst], kUniqueOverflow);
     const bool over = __any_sync(0xffffffffu, r < 0);
     if (over && lane == 0)
         atomicOr(a.status, kStatusTableOverflow);
@@ -318,11 +324,7 @@ __device__ __forceinline__ bool flush_children(const ExpandArgs &a, const WarpSt
     const unsigned peers = __match_any_sync(0xffffffffu, fresh ? inst : 0xFFFFFFFFu);
     if (fresh && lane == (unsigned)(__ffs(peers) - 1))
         atomicAdd(&a.inst_unique[inst], (unsigned)__popc(peers));
-    unsigned int stt = 0;
-    if (lane == 0)
-        stt = __ldcg(a.status);
-    stt = __shfl_sync(0xffffffffu, stt, 0);
-    return over || (stt & kStatusTableOverflow) != 0u;
+    return r < 0 ? inst : 0xFFFFFFFFu;
 }
 
 // Expansion.  Warps work independently (no block barrier): each warp takes
@@ -338,7 +340,7 @@ __device__ __forceinline__ bool flush_children(const ExpandArgs &a, const WarpSt
 // Completed rows are staged in shared memory and inserted by the whole
 // warp, 32 at a time.
 template <bool K64>
-__global__ void __launch_bounds__(kExpandBlock)
+__global__ void __launch_bounds__(kExpandBlock, 4)
 k_expand(ExpandArgs a) {
     __shared__ WarpStage stage[kWarps];
     const unsigned lane = threadIdx.x & 31u;
@@ -371,14 +373,10 @@ k_expand(ExpandArgs a) {
         while (need && !no_more) {
             if (c_next >= c_end) {
                 unsigned long long ci = 0;
-                unsigned int stt = 0;
-                if (lane == 0) {
+                if (lane == 0)
                     ci = atomicAdd(a.work, 1ull);
-                    stt = __ldcg(a.status);
-                }
                 ci = __shfl_sync(0xffffffffu, ci, 0);
-                stt = __shfl_sync(0xffffffffu, stt, 0);
-                if (ci >= a.n_chunks || (stt & kStatusTableOverflow)) {
+                if (ci >= a.n_chunks) {
                     no_more = true;
                     break;
                 }
@@ -396,10 +394,16 @@ k_expand(ExpandArgs a) {
                 c_next = s.begin + (ci - s.chunk_base) * a.chunk_states;
                 const unsigned long long se = s.begin + s.len;
                 c_end = c_next + a.chunk_states < se ? c_next + a.chunk_states : se;
-                // An instance past its frontier limit fails anyway: skip the
-                // rest of its work.
+                // An instance past its frontier limit fails anyway, and one
+                // whose table region overflowed is redone: skip its work.
+                // The counter changes under other warps, so one lane reads
+                // it and the decision stays warp-uniform.
                 const uint32_t lim = a.insts[s.inst].limit;
-                if (lim && __ldcg(a.inst_unique + s.inst) > lim)
+                uint32_t un = 0;
+                if (lane == 0)
+                    un = __ldcg(a.inst_unique + s.inst);
+                un = __shfl_sync(0xffffffffu, un, 0);
+                if ((un & kUniqueOverflow) || (lim && un > lim))
                     c_next = c_end;
             }
             const unsigned long long avail = c_end - c_next;
@@ -613,18 +617,24 @@ k_expand(ExpandArgs a) {
             ws.k0[pos] = ck0;
             ws.k1[pos] = ck1;
             ws.cnt[pos] = cnt;
-            ws.inst[pos] = sg->inst | (wit ? 0x80000000u : 0u);
+            ws.seg[pos] = (uint32_t)(sg - a.segs) | (wit ? 0x80000000u : 0u);
             ++raw;
         }
         nbuf += __popc(em);
         if (nbuf >= 32) {
             __syncwarp();
-            const bool over = flush_children<K64>(a, ws, nbuf - 32, 32, lane);
+            const uint32_t failed = flush_children<K64>(a, ws, nbuf - 32, 32, lane);
             nbuf -= 32;
             __syncwarp();
-            if (over) {
-                nbuf = 0;   // the level is redone: drop the rest
-                break;
+            // Lanes walking an instance whose region just overflowed stop
+            // (its row is redone); rare, so the 32-way compare is cheap.
+            if (__any_sync(0xffffffffu, failed != 0xFFFFFFFFu)) {
+                const uint32_t mine = active ? sg->inst : 0xFFFFFFFEu;
+                bool hit = false;
+                for (int q = 0; q < 32; q++)
+                    hit |= __shfl_sync(0xffffffffu, failed, q) == mine;
+                if (hit)
+                    active = false;
             }
         }
     }

@@ -218,6 +218,8 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
                     hi |= (unsigned long long)inst->rows[row + i] << (i * W);
             sg.hi_board = hi;
             sg.tag = tag;
+            sg.tbase = 0;
+            sg.tcap = L.cap_slots;
             const uint32_t fan = n * 4 < slots * 256 && fan_max > 1 ? fan_max : 0;
             const uint64_t items = n * (fan ? fan : 1);
             const uint64_t warps = slots * 8;

@@ -216,19 +216,38 @@ private:
         try {
             cuda_check(cudaSetDevice(opts_.device), "cudaSetDevice");
             for (;;) {
+                const auto ta = Clock::now();
                 admit(l);
+                {
+                    std::lock_guard<std::mutex> lk(mu_);
+                    st_.lane_admit_ms[l] += ms_between(ta, Clock::now());
+                }
                 bool busy = false;
                 for (int e = 0; e < 2; e++) {
                     if (!ln.eng[e]->has_active())
                         continue;
                     busy = true;
                     const auto t0 = Clock::now();
-                    const uint64_t restarts0 = ln.eng[e]->totals().restarts;
+                    const Totals before = ln.eng[e]->totals();
+                    const uint64_t restarts0 = before.restarts;
                     const size_t n_run = ln.running[e].size();
                     const StepStats s = ln.eng[e]->step();
                     const auto t1 = Clock::now();
                     collect(l, e);
+                    const auto t2 = Clock::now();
+                    const Totals &after = ln.eng[e]->totals();
                     std::lock_guard<std::mutex> lk(mu_);
+                    st_.lane_collect_ms[l] += ms_between(t1, t2);
+                    st_.lane_upload_ms[l] += after.upload_ms - before.upload_ms;
+                    st_.lane_solve_one_ms[l] += (after.keep_ms - before.keep_ms) +
+                                                (after.trace_ms - before.trace_ms);
+                    st_.lane_retries[l] += after.retries - before.retries;
+                    st_.lane_phase_ms[l][0] += after.ph_select_ms - before.ph_select_ms;
+                    st_.lane_phase_ms[l][1] += after.ph_table_ms - before.ph_table_ms;
+                    st_.lane_phase_ms[l][2] += after.ph_expand_ms - before.ph_expand_ms;
+                    st_.lane_phase_ms[l][3] += after.ph_post_ms - before.ph_post_ms;
+                    st_.lane_phase_ms[l][4] += after.ph_compact_ms - before.ph_compact_ms;
+                    st_.lane_phase_ms[l][5] += after.ph_tail_ms - before.ph_tail_ms;
                     st_.steps++;
                     st_.states_out += s.n_out;
                     st_.busy_ms += ms_between(t0, t1);

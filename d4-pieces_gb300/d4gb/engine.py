@@ -76,10 +76,13 @@ class Stats(C.Structure):
         ("tuned_ctas_per_sm", C.c_uint64),
         ("tuned_load", C.c_double),
         ("compact_slots", C.c_uint64),
+        ("phase_ms", C.c_double * 6),
     ]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["phase_ms"] = list(self.phase_ms)
+        return d
 
 
 class BatchOpts(C.Structure):
@@ -147,11 +150,20 @@ class ServerStats(C.Structure):
         ("lane_inst_rows", C.c_uint64 * 2),
         ("restarts", C.c_uint64),
         ("paused", C.c_uint64),
+        ("lane_admit_ms", C.c_double * 2),
+        ("lane_collect_ms", C.c_double * 2),
+        ("lane_upload_ms", C.c_double * 2),
+        ("lane_solve_one_ms", C.c_double * 2),
+        ("lane_retries", C.c_uint64 * 2),
+        ("lane_phase_ms", (C.c_double * 6) * 2),
     ]
 
     def as_dict(self) -> dict:
-        return {k: (list(v) if not isinstance(v := getattr(self, k), (int, float)) else v)
-                for k, _ in self._fields_}
+        def plain(v):
+            if isinstance(v, (int, float)):
+                return v
+            return [plain(x) for x in v]
+        return {k: plain(getattr(self, k)) for k, _ in self._fields_}
 
 
 class Instance(C.Structure):

@@ -185,6 +185,9 @@ typedef struct d4e_stats {
     uint64_t tuned_ctas_per_sm; /* k_expand CTAs per SM (0 = occupancy) */
     double tuned_load;          /* hash table load factor */
     uint64_t compact_slots;     /* hash-table slots scanned by k_compact (all launches) */
+    double phase_ms[6];         /* host wall time inside row steps: selecting instances,
+                                   preparing tables, waiting for k_expand, bookkeeping,
+                                   waiting for k_compact, row tail */
 } d4e_stats;
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st);
@@ -323,6 +326,12 @@ typedef struct d4e_server_stats {
     uint64_t lane_inst_rows[2]; /* per lane: instance-rows advanced */
     uint64_t restarts;          /* solve-one attempts redone with a wider sample */
     uint64_t paused;            /* instance-rows that waited for memory */
+    double lane_admit_ms[2];    /* per lane: admitting requests (placement tables built) */
+    double lane_collect_ms[2];  /* per lane: handing out finished results */
+    double lane_upload_ms[2];   /* per lane, inside steps: uploading new instances */
+    double lane_solve_one_ms[2];/* per lane, inside steps: keeping levels + tracing */
+    uint64_t lane_retries[2];   /* per lane: table-region overflows redone */
+    double lane_phase_ms[2][6]; /* per lane: the row-step phases of d4e_stats.phase_ms */
 } d4e_server_stats;
 
 int d4e_server_stats_get(d4e_server *s, d4e_server_stats *st);
