@@ -67,8 +67,10 @@ def parse_args():
     ap.add_argument("--cpu-budget", type=float, default=15.0,
                     help="seconds of host CPU work for the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-autotune", action="store_true",
-                    help="skip the launch autotuner (it runs in the first warm-up step)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="measure launch plans in the first warm-up step (D4E_AUTOTUNE); "
+                         "the default plan is the one the tuner keeps on this workload")
+    ap.add_argument("--no-autotune", action="store_true", help=argparse.SUPPRESS)
     return ap.parse_args()
 
 
@@ -211,7 +213,7 @@ def profiled_traffic() -> dict | None:
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
-def run_once(E, prob, device: int, autotune: bool = True) -> dict:
+def run_once(E, prob, device: int, autotune: bool = False) -> dict:
     t0 = time.perf_counter()
     f = E.Frow(prob.shapes, prob.counts, prob.sym, prob.width, device=device)
     s = E.CudaSearcher(f, rows=prob.rows, autotune=autotune)
@@ -256,7 +258,7 @@ def bench_ours(args, dist: Dist) -> None:
     dev = dist.local_rank
     prob, workload = make_problem(args)
     for _ in range(args.warmup):
-        run_once(E, prob, dev, not args.no_autotune)
+        run_once(E, prob, dev, args.autotune and not args.no_autotune)
     flush_l2(dev)
     dist.barrier()
     sampler = ClockSampler(dev)
@@ -264,7 +266,7 @@ def bench_ours(args, dist: Dist) -> None:
     runs = []
     t_start = time.perf_counter()
     for _ in range(args.steps):
-        runs.append(run_once(E, prob, dev, not args.no_autotune))
+        runs.append(run_once(E, prob, dev, args.autotune and not args.no_autotune))
         flush_l2(dev)
     t_wall = time.perf_counter() - t_start
     clocks = sampler.stop()
@@ -327,7 +329,7 @@ def bench_ours(args, dist: Dist) -> None:
             "states_per_step": states // args.steps,
             "raw_children_per_step": sum(s["states_raw"] for s in st) // args.steps,
             "record_bytes": st[0]["record_bytes"],
-            "launch_plan": {"autotuned": not args.no_autotune,
+            "launch_plan": {"autotuned": args.autotune and not args.no_autotune,
                             "chunk_cap": st[0]["tuned_chunk_cap"],
                             "chunks_per_warp": st[0]["tuned_chunks_per_warp"],
                             "ctas_per_sm": st[0]["tuned_ctas_per_sm"] or "occupancy",
