@@ -71,12 +71,13 @@ __device__ __forceinline__ void merge_value(unsigned long long *v, unsigned long
         atomicAdd(v, x);
 }
 
-// Insert with multiplicity cnt (linear probing).  Returns 1 for a newly
-// claimed key, 0 for an existing one, -1 when the probe limit was reached.
-__device__ __forceinline__ int insert64(Slot16 *__restrict__ T, unsigned long long cap,
-                                        unsigned long long key, unsigned long long cnt,
-                                        unsigned int max_probe, bool wmax = false) {
-    unsigned long long h = home64(key, cap);
+// Insert with multiplicity cnt (linear probing from slot h).  Returns 1
+// for a newly claimed key, 0 for an existing one, -1 when the probe limit
+// was reached.
+__device__ __forceinline__ int insert64_at(Slot16 *__restrict__ T, unsigned long long cap,
+                                           unsigned long long h, unsigned long long key,
+                                           unsigned long long cnt, unsigned int max_probe,
+                                           bool wmax) {
     for (unsigned int p = 0; p < max_probe; ++p) {
         // A naturally aligned 8-byte load is single-copy atomic: a key seen
         // here is final.  Only an empty slot needs the CAS.
@@ -97,11 +98,16 @@ __device__ __forceinline__ int insert64(Slot16 *__restrict__ T, unsigned long lo
     return -1;
 }
 
-__device__ __forceinline__ int insert128(Slot32 *__restrict__ T, unsigned long long cap,
-                                         unsigned long long k0, unsigned long long k1,
-                                         unsigned long long cnt, unsigned int max_probe,
-                                         bool wmax = false) {
-    unsigned long long h = home128(k0, k1, cap);
+__device__ __forceinline__ int insert64(Slot16 *__restrict__ T, unsigned long long cap,
+                                        unsigned long long key, unsigned long long cnt,
+                                        unsigned int max_probe, bool wmax = false) {
+    return insert64_at(T, cap, home64(key, cap), key, cnt, max_probe, wmax);
+}
+
+__device__ __forceinline__ int insert128_at(Slot32 *__restrict__ T, unsigned long long cap,
+                                            unsigned long long h, unsigned long long k0,
+                                            unsigned long long k1, unsigned long long cnt,
+                                            unsigned int max_probe, bool wmax) {
     for (unsigned int p = 0; p < max_probe; ++p) {
         unsigned long long o0, o1;
         cas128(&T[h].k0, 0ull, 0ull, k0, k1, o0, o1);
@@ -113,6 +119,13 @@ __device__ __forceinline__ int insert128(Slot32 *__restrict__ T, unsigned long l
         h = next_slot(h, cap);
     }
     return -1;
+}
+
+__device__ __forceinline__ int insert128(Slot32 *__restrict__ T, unsigned long long cap,
+                                         unsigned long long k0, unsigned long long k1,
+                                         unsigned long long cnt, unsigned int max_probe,
+                                         bool wmax = false) {
+    return insert128_at(T, cap, home128(k0, k1, cap), k0, k1, cnt, max_probe, wmax);
 }
 
 
@@ -287,6 +300,7 @@ struct WarpStage {
     unsigned long long k0[kStage];
     unsigned long long k1[kStage];
     unsigned long long cnt[kStage];
+    unsigned long long home[kStage];   // home slot within the instance's region
     uint32_t seg[kStage];   // producing segment | witness flag (bit 31)
 };
 
@@ -307,12 +321,16 @@ __device__ __forceinline__ uint32_t flush_children(const ExpandArgs &a, const Wa
         const bool wmax = (si >> 31) != 0u;   // solve-one instance: value = witness
         const Seg &s = a.segs[si & 0x7FFFFFFFu];
         inst = s.inst;
-        if constexpr (K64)
-            r = insert64(static_cast<Slot16 *>(a.table) + s.tbase, s.tcap, ws.k0[j], ws.cnt[j],
-                         a.max_probe, wmax);
-        else
-            r = insert128(static_cast<Slot32 *>(a.table) + s.tbase, s.tcap, ws.k0[j], ws.k1[j],
-                          ws.cnt[j], a.max_probe, wmax);
+        if constexpr (K64) {
+            const unsigned long long h = a.prefetch ? ws.home[j] : home64(ws.k0[j], s.tcap);
+            r = insert64_at(static_cast<Slot16 *>(a.table) + s.tbase, s.tcap, h, ws.k0[j],
+                            ws.cnt[j], a.max_probe, wmax);
+        } else {
+            const unsigned long long h =
+                a.prefetch ? ws.home[j] : home128(ws.k0[j], ws.k1[j], s.tcap);
+            r = insert128_at(static_cast<Slot32 *>(a.table) + s.tbase, s.tcap, h, ws.k0[j],
+                             ws.k1[j], ws.cnt[j], a.max_probe, wmax);
+        }
     }
     if (r < 0)
         atomicOr(&a.inst_unique[inst], kUniqueOverflow);
@@ -618,6 +636,23 @@ k_expand(ExpandArgs a) {
             ws.k1[pos] = ck1;
             ws.cnt[pos] = cnt;
             ws.seg[pos] = (uint32_t)(sg - a.segs) | (wit ? 0x80000000u : 0u);
+            // The child's home slot; for moderate tables its line is also
+            // requested into L2 now, so the insert at the next flush finds it
+            // there (on tables of many GB the extra line fills cost more
+            // HBM bandwidth than the latency they hide: the host turns it
+            // off).
+            if (a.prefetch) {
+                // (Only then: hashing here, on the few lanes that emit, costs
+                // more issue slots than hashing in the converged flush.)
+                const unsigned long long hr =
+                    K64 ? home64(ck0, sg->tcap) : home128(ck0, ck1, sg->tcap);
+                ws.home[pos] = hr;
+                const void *line = K64 ? (const void *)(static_cast<const Slot16 *>(a.table) +
+                                                        sg->tbase + hr)
+                                       : (const void *)(static_cast<const Slot32 *>(a.table) +
+                                                        sg->tbase + hr);
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(line));
+            }
             ++raw;
         }
         nbuf += __popc(em);

@@ -31,6 +31,7 @@ struct ExpandArgs {
     unsigned int *status;
     unsigned long long *work;        // dynamic chunk counter, zeroed before launch
     unsigned int max_probe;
+    uint32_t prefetch;               // request each child's table line into L2 when staged
 };
 
 struct CompactArgs {
