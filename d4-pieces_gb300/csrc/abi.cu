@@ -185,6 +185,10 @@ static int make_searcher(const d4e_frow *f, uint32_t height, const uint8_t *rows
     o.device = f->device;
     o.keep_levels = (flags & D4E_KEEP_LEVELS) != 0;
     o.autotune = (flags & D4E_AUTOTUNE) != 0;
+    if (flags & D4E_DEDUP_DIRECT)
+        o.dedup = d4e::EngineOpts::Dedup::Direct;
+    if (flags & D4E_DEDUP_PARTITIONED)
+        o.dedup = d4e::EngineOpts::Dedup::Partitioned;
     s->eng = std::make_unique<d4e::Engine>(o);
     d4e::InstanceSpec sp;
     sp.width = f->width;
@@ -360,6 +364,9 @@ static void fill_stats(const d4e::Engine &e, d4e_stats *st, bool add = false) {
                           t.ph_compact_ms, t.ph_tail_ms};
     for (int i = 0; i < 6; i++)
         st->phase_ms[i] += ph[i];
+    st->partitioned += t.partitioned;
+    st->partition_fallbacks += t.partition_fallbacks;
+    st->merge_ms += t.merge_ms;
 }
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st) {
@@ -507,6 +514,10 @@ int d4e_batch_run(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *o
         if (o.flags & D4E_BATCH_WIDE_KEYS)
             eo.key_mode = d4e::KeyMode::K128;
         eo.autotune = (o.flags & D4E_BATCH_AUTOTUNE) != 0;
+        if (o.flags & D4E_BATCH_DEDUP_DIRECT)
+            eo.dedup = d4e::EngineOpts::Dedup::Direct;
+        if (o.flags & D4E_BATCH_DEDUP_PARTITIONED)
+            eo.dedup = d4e::EngineOpts::Dedup::Partitioned;
         if (st)
             std::memset(st, 0, sizeof(*st));
         if (o.flags & D4E_BATCH_SEQUENTIAL) {

@@ -128,7 +128,13 @@ struct alignas(16) Slot16 {
 enum : uint32_t {
     kStatusTableOverflow = 1u,    // probe limit reached: table too small, level is redone
     kStatusNodeOverflow = 2u,     // solution path buffer full
+    kStatusBucketOverflow = 4u,   // partitioned dedup: a bucket or its on-chip table was full
 };
+
+// Partitioned dedup: on-chip table slots per bucket (k_bucket_merge) and the
+// distinct states a bucket is sized for.
+constexpr unsigned kBucketSlots = 4096;
+constexpr unsigned kBucketTarget = 1536;
 
 // Cursor value marking an instance whose row being completed is its last:
 // its states are summed into the per-instance result instead of stored.

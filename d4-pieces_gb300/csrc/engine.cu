@@ -218,6 +218,9 @@ Engine::~Engine() {
     trace_out_.release();
     chain_.release();
     tsegs_.release();
+    bkt_recs_.release();
+    bkt_cnt_.release();
+    dtab_.release();
     for (auto p : lvl_keys_)
         cudaFree(p);
     for (auto p : lvl_cnts_)
@@ -847,7 +850,116 @@ StepStats Engine::step_impl() {
             tot_.splits++;
             continue;
         }
+        // Large packed-key rows: partitioned de-duplication (children
+        // appended into hash buckets, each bucket merged in shared memory)
+        // instead of random inserts into a table far larger than L2.
+        bool part = false;
+        uint64_t n_bkt = 0, bkt_cap = 0;
+        const bool want_part = opts_.dedup == EngineOpts::Dedup::Partitioned;
+        if (want_part && k64_ && raw_ratio_ > 0.0) {
+            n_bkt = std::max<uint64_t>(1, (uint64_t)(est * 1.25 / kBucketTarget) + 1);
+            const double est_raw = (double)n_grp * raw_ratio_ * 1.25;
+            bkt_cap = round_up((uint64_t)(est_raw / (double)n_bkt * 1.5) + 256, 64);
+            const double bytes = (double)n_bkt * (double)bkt_cap * 16.0 +
+                                 (double)n_bkt * kBucketSlots * 16.0 + (double)n_bkt * 4.0 +
+                                 est * 16.0;
+            part = bytes <= (double)limit * (16.0 + 16.0 * tune_.load);
+        }
+        unsigned long long h_raw = 0;
+        float part_ms = 0.f, merge_ms = 0.f;
+        if (part) {
+            if (!merge_ready_) {
+                cuda_check(bucket_merge_prepare(), "cudaFuncSetAttribute");
+                merge_ready_ = true;
+            }
+            bkt_recs_.reserve(n_bkt * bkt_cap, stream_);
+            bkt_cnt_.reserve(n_bkt, stream_);
+            dtab_.reserve(n_bkt * kBucketSlots, stream_);
+            cuda_check(cudaMemsetAsync(bkt_cnt_.p, 0, n_bkt * sizeof(unsigned int), stream_),
+                       "memset");
+            cuda_check(cudaMemsetAsync(inst_unique_.p, 0, n_inst * sizeof(unsigned int), stream_),
+                       "memset");
+            cuda_check(cudaMemsetAsync(misc_.p, 0, 4 * sizeof(unsigned int), stream_), "memset");
+            cuda_check(cudaMemsetAsync(nraw_.p, 0, 2 * sizeof(unsigned long long), stream_),
+                       "memset");
+            phase(tot_.ph_table_ms);
+            ExpandArgs a{};
+            a.segs = segs_.p;
+            a.n_segs = (uint32_t)segs.size();
+            a.n_chunks = n_chunks;
+            a.chunk_states = chunk;
+            a.fan = fan;
+            a.insts = insts_.p;
+            a.plc = plc_.p;
+            a.filt = filt_.p;
+            a.recs = keys_[cur_].p;
+            a.cnts = cnts_[cur_].p;
+            a.table = table_.p;
+            a.cap = 0;
+            a.inst_unique = inst_unique_.p;
+            a.n_raw = nraw_.p;
+            a.status = misc_.p;
+            a.work = nraw_.p + 1;
+            a.max_probe = opts_.max_probe;
+            a.append = 1;
+            a.bkt_recs = bkt_recs_.p;
+            a.bkt_cnt = bkt_cnt_.p;
+            a.n_bkt = n_bkt;
+            a.bkt_cap = bkt_cap;
+            cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
+            launch_expand(k64_, a, grid, stream_);
+            cuda_check(cudaGetLastError(), "k_expand launch");
+            cuda_check(cudaEventRecord(ev_[1], stream_), "cudaEventRecord");
+            tot_.expand_launches++;
+            MergeArgs m{};
+            m.bkt_recs = bkt_recs_.p;
+            m.bkt_cnt = bkt_cnt_.p;
+            m.n_bkt = n_bkt;
+            m.bkt_cap = bkt_cap;
+            m.dtab = reinterpret_cast<Slot16 *>(dtab_.p);
+            m.insts = insts_.p;
+            m.inst_off = inst_off_;
+            m.inst_mask = inst_mask_;
+            m.inst_unique = inst_unique_.p;
+            m.status = misc_.p;
+            launch_bucket_merge(m, sms_ * 3, stream_);
+            cuda_check(cudaGetLastError(), "k_bucket_merge launch");
+            cuda_check(cudaEventRecord(ev_[2], stream_), "cudaEventRecord");
+            tot_.other_launches++;
+            unsigned int h_status = 0;
+            cuda_check(cudaMemcpyAsync(&h_status, misc_.p, sizeof(unsigned int),
+                                       cudaMemcpyDeviceToHost, stream_),
+                       "read status");
+            cuda_check(cudaMemcpyAsync(&h_raw, nraw_.p, sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost, stream_),
+                       "read raw");
+            h_grp_unique_.resize(n_inst);
+            cuda_check(cudaMemcpyAsync(h_grp_unique_.data(), inst_unique_.p,
+                                       n_inst * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                       stream_),
+                       "read unique");
+            cuda_check(cudaStreamSynchronize(stream_), "k_expand + k_bucket_merge");
+            phase(tot_.ph_expand_ms);
+            cudaEventElapsedTime(&part_ms, ev_[0], ev_[1]);
+            cudaEventElapsedTime(&merge_ms, ev_[1], ev_[2]);
+            st.expand_ms += part_ms;
+            tot_.merge_ms += merge_ms;
+            st.compact_ms += merge_ms;
+            if (h_raw && n_grp)
+                raw_ratio_ = (double)h_raw / (double)n_grp;
+            if (h_status & kStatusBucketOverflow) {
+                // A bucket (or its on-chip table) was too small: redo the row
+                // with the direct table.
+                part = false;
+                tot_.partition_fallbacks++;
+                st.retries++;
+                tot_.retries++;
+            } else {
+                tot_.partitioned++;
+            }
+        }
         const uint64_t units = cap * slot_units();
+        if (!part) {
         if (table_.cap < units) {
             table_.release();
             table_clean_ = 0;
@@ -864,7 +976,7 @@ StepStats Engine::step_impl() {
         cuda_check(cudaMemsetAsync(misc_.p, 0, 4 * sizeof(unsigned int), stream_), "memset");
         cuda_check(cudaMemsetAsync(nraw_.p, 0, 2 * sizeof(unsigned long long), stream_), "memset");
         phase(tot_.ph_table_ms);
-        ExpandArgs a;
+        ExpandArgs a{};
         a.segs = segs_.p;
         a.n_segs = (uint32_t)segs.size();
         a.n_chunks = n_chunks;
@@ -888,7 +1000,6 @@ StepStats Engine::step_impl() {
         cuda_check(cudaGetLastError(), "k_expand launch");
         cuda_check(cudaEventRecord(ev_[1], stream_), "cudaEventRecord");
         tot_.expand_launches++;
-        unsigned long long h_raw = 0;
         cuda_check(cudaMemcpyAsync(&h_raw, nraw_.p, sizeof(unsigned long long),
                                    cudaMemcpyDeviceToHost, stream_),
                    "read raw");
@@ -898,12 +1009,19 @@ StepStats Engine::step_impl() {
                    "read unique");
         cuda_check(cudaStreamSynchronize(stream_), "k_expand");
         phase(tot_.ph_expand_ms);
-        tot_.d2h_bytes += sizeof(unsigned long long) + n_inst * sizeof(unsigned int);
         {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
             st.expand_ms += ms;
         }
+        if (h_raw && n_grp)
+            raw_ratio_ = (double)h_raw / (double)n_grp;
+        }
+        tot_.d2h_bytes += sizeof(unsigned long long) + n_inst * sizeof(unsigned int);
+        // The table k_compact reads: the merged bucket tables, or the
+        // instances' regions.
+        void *ctab = part ? (void *)dtab_.p : (void *)table_.p;
+        const uint64_t ccap = part ? n_bkt * kBucketSlots : cap;
         st.groups++;
         st.n_raw += h_raw;
         st.table_cap = std::max<uint64_t>(st.table_cap, cap);
@@ -1013,8 +1131,8 @@ StepStats Engine::step_impl() {
             tot_.h2d_bytes += n_inst * sizeof(unsigned long long);
         }
         CompactArgs c;
-        c.table = table_.p;
-        c.cap = cap;
+        c.table = ctab;
+        c.cap = ccap;
         c.cursor = cursor_.p;
         c.out_recs = keys_[nxt].p;
         c.out_cnts = cnts_[nxt].p;
@@ -1023,14 +1141,14 @@ StepStats Engine::step_impl() {
         c.inst_off = inst_off_;
         c.inst_mask = inst_mask_;
         c.keep_max = sampled.empty() ? nullptr : keep_max_.p;
-        const int cgrid = compact_grid(cap, sms_);
+        const int cgrid = compact_grid(ccap, sms_);
         phase(tot_.ph_post_ms);
         cuda_check(cudaEventRecord(ev_[2], stream_), "cudaEventRecord");
         launch_compact(k64_, c, cgrid, stream_);
         cuda_check(cudaGetLastError(), "k_compact launch");
         cuda_check(cudaEventRecord(ev_[3], stream_), "cudaEventRecord");
         tot_.compact_launches++;
-        tot_.compact_slots += cap;
+        tot_.compact_slots += ccap;
         cuda_check(cudaStreamSynchronize(stream_), "k_compact");
         phase(tot_.ph_compact_ms);
         float cms = 0.f;

@@ -100,6 +100,14 @@ struct EngineOpts {
     // Measure launch plans on the first row of 2^21..2^25 states and keep
     // the fastest (cached per key encoding, board width and device).
     bool autotune = false;
+    // De-duplication of a row's children: Direct (Auto) inserts them into
+    // the hash table as they are produced; Partitioned appends them into
+    // hash buckets and merges each bucket on chip (packed keys, after the
+    // first row; a bucket overflow redoes the row directly).  Measured on
+    // the 8x15 enumeration, appending did not shorten k_expand (56 ms per
+    // launch either way: the walk, not the insert, bounds it) and the merge
+    // added ~200 ms, so Auto stays direct.
+    enum class Dedup { Auto, Direct, Partitioned } dedup = Dedup::Auto;
 };
 
 // Launch plan of k_expand / k_compact and the table's load factor.
@@ -157,6 +165,9 @@ struct Totals {
     double ph_select_ms = 0.0, ph_table_ms = 0.0, ph_expand_ms = 0.0, ph_post_ms = 0.0,
            ph_compact_ms = 0.0, ph_tail_ms = 0.0;
     uint64_t compact_slots = 0;    // table slots scanned by k_compact (sum over launches)
+    uint64_t partitioned = 0;      // groups de-duplicated through buckets
+    uint64_t partition_fallbacks = 0;   // ... of which redone with the direct table
+    double merge_ms = 0.0;         // device time of k_bucket_merge
 };
 
 // One kept frontier level of a solve-one instance: `len` records from
@@ -313,6 +324,13 @@ private:
     uint64_t n_cur_ = 0;
 
     DevBuf<ulonglong2> table_;    // slot_units() 16-byte units per slot
+    // Partitioned dedup buffers: bucketed raw children, bucket counters,
+    // merged bucket tables.
+    DevBuf<ulonglong2> bkt_recs_;
+    DevBuf<unsigned int> bkt_cnt_;
+    DevBuf<ulonglong2> dtab_;
+    double raw_ratio_ = 0.0;      // raw children per input state, last group
+    bool merge_ready_ = false;
     uint64_t table_clean_ = 0;    // units [0, table_clean_) are known to be zero
     double growth_ = 8.0;
 

@@ -315,6 +315,23 @@ __device__ __forceinline__ uint32_t flush_children(const ExpandArgs &a, const Wa
     // Lane i inserts child base + i: up to 32 independent inserts in flight.
     int r = 2;
     uint32_t inst = 0xFFFFFFFFu;
+    if constexpr (K64) {
+        if (a.append) {
+            // Partitioned dedup: append to the child's bucket (the bucket
+            // counters are few enough to stay in L2).
+            if ((int)lane < n) {
+                const int j = base + (int)lane;
+                const unsigned long long key = ws.k0[j];
+                const unsigned long long b = __umul64hi(mix64(key), a.n_bkt);
+                const unsigned int pos = atomicAdd(a.bkt_cnt + b, 1u);
+                if (pos < a.bkt_cap)
+                    a.bkt_recs[b * a.bkt_cap + pos] = make_ulonglong2(key, ws.cnt[j]);
+                else
+                    atomicOr(a.status, kStatusBucketOverflow);
+            }
+            return 0xFFFFFFFFu;
+        }
+    }
     if ((int)lane < n) {
         const int j = base + (int)lane;
         const uint32_t si = ws.seg[j];
@@ -987,6 +1004,79 @@ k_extend_paths(ProbeArgs p, const PathNode *__restrict__ nodes, uint32_t n_nodes
     }
 }
 
+// Partitioned dedup, second half: one bucket per block iteration.
+constexpr int kMergeBlock = 512;
+constexpr unsigned kMergeProbe = 256;
+
+__global__ void __launch_bounds__(kMergeBlock)
+k_bucket_merge(MergeArgs m) {
+    extern __shared__ Slot16 tab[];   // kBucketSlots slots
+    __shared__ unsigned int s_over;
+    const unsigned lane = threadIdx.x & 31u;
+    for (unsigned i = threadIdx.x; i < kBucketSlots; i += blockDim.x)
+        tab[i] = Slot16{0ull, 0ull};
+    if (threadIdx.x == 0)
+        s_over = 0;
+    __syncthreads();
+    for (unsigned long long b = blockIdx.x; b < m.n_bkt; b += gridDim.x) {
+        const unsigned int n = min(m.bkt_cnt[b], (unsigned int)m.bkt_cap);
+        const ulonglong2 *recs = m.bkt_recs + b * m.bkt_cap;
+        for (unsigned int base = 0; base < n; base += blockDim.x) {
+            const unsigned int i = base + threadIdx.x;
+            int r = 2;
+            uint32_t inst = 0xFFFFFFFFu;
+            if (i < n) {
+                const ulonglong2 rec = recs[i];
+                inst = (uint32_t)((rec.x >> m.inst_off) & m.inst_mask);
+                const bool wmax = (m.insts[inst].flags & kInstWitness) != 0u;
+                // Bucket = high bits of the hash; the slot = its low bits.
+                unsigned h = (unsigned)mix64(rec.x) & (kBucketSlots - 1u);
+                r = -1;
+                for (unsigned p = 0; p < kMergeProbe; ++p) {
+                    unsigned long long k = *reinterpret_cast<volatile unsigned long long *>(&tab[h].key);
+                    if (k == 0ull) {
+                        k = atomicCAS(&tab[h].key, 0ull, rec.x);
+                        if (k == 0ull) {
+                            if (wmax)
+                                atomicMax(&tab[h].cnt, rec.y);
+                            else
+                                atomicAdd(&tab[h].cnt, rec.y);
+                            r = 1;
+                            break;
+                        }
+                    }
+                    if (k == rec.x) {
+                        if (wmax)
+                            atomicMax(&tab[h].cnt, rec.y);
+                        else
+                            atomicAdd(&tab[h].cnt, rec.y);
+                        r = 0;
+                        break;
+                    }
+                    h = (h + 1u) & (kBucketSlots - 1u);
+                }
+                if (r < 0)
+                    s_over = 1;
+            }
+            // New keys per instance, warp-aggregated.
+            const bool fresh = r == 1;
+            const unsigned peers = __match_any_sync(0xffffffffu, fresh ? inst : 0xFFFFFFFFu);
+            if (fresh && lane == (unsigned)(__ffs(peers) - 1))
+                atomicAdd(&m.inst_unique[inst], (unsigned)__popc(peers));
+        }
+        __syncthreads();
+        // The bucket's table, empties included, is its slice of dtab.
+        Slot16 *out = m.dtab + b * kBucketSlots;
+        for (unsigned i = threadIdx.x; i < kBucketSlots; i += blockDim.x) {
+            out[i] = tab[i];
+            tab[i] = Slot16{0ull, 0ull};
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && s_over)
+        atomicOr(m.status, kStatusBucketOverflow);
+}
+
 __global__ void k_select(const ulonglong2 *__restrict__ recs, const unsigned char *__restrict__ alive,
                          unsigned long long n, ulonglong2 *__restrict__ out,
                          unsigned long long *__restrict__ n_out) {
@@ -1099,6 +1189,17 @@ void launch_count_pattern(const ulonglong2 *recs, unsigned long long n, unsigned
     if (n == 0)
         return;
     k_count_pattern<<<grid, 256, 0, s>>>(recs, n, mask, value, out);
+}
+
+cudaError_t bucket_merge_prepare() {
+    return cudaFuncSetAttribute(k_bucket_merge, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(kBucketSlots * sizeof(Slot16)));
+}
+
+void launch_bucket_merge(const MergeArgs &m, int grid, cudaStream_t s) {
+    if (m.n_bkt == 0)
+        return;
+    k_bucket_merge<<<grid, kMergeBlock, kBucketSlots * sizeof(Slot16), s>>>(m);
 }
 
 }  // namespace d4e

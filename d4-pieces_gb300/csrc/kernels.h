@@ -32,7 +32,32 @@ struct ExpandArgs {
     unsigned long long *work;        // dynamic chunk counter, zeroed before launch
     unsigned int max_probe;
     uint32_t prefetch;               // request each child's table line into L2 when staged
+    // Partitioned dedup (K64 only): children are appended to bucket
+    // hi(hash(key) * n_bkt) instead of inserted into the table; bucket b
+    // holds records [b * bkt_cap, b * bkt_cap + bkt_cnt[b]).
+    uint32_t append;
+    ulonglong2 *bkt_recs;
+    unsigned int *bkt_cnt;
+    unsigned long long n_bkt, bkt_cap;
 };
+
+// De-duplicates every bucket in an on-chip table (counts summed, witnesses
+// maxed), adds each bucket's new keys to inst_unique, and writes the
+// bucket's table of kBucketSlots slots to dtab[b * kBucketSlots ...]
+// (empty slots zero), which k_compact then turns into the next frontier.
+struct MergeArgs {
+    const ulonglong2 *bkt_recs;
+    const unsigned int *bkt_cnt;
+    unsigned long long n_bkt, bkt_cap;
+    Slot16 *dtab;
+    const InstDesc *insts;
+    uint32_t inst_off;
+    unsigned long long inst_mask;
+    unsigned int *inst_unique;
+    unsigned int *status;
+};
+void launch_bucket_merge(const MergeArgs &m, int grid, cudaStream_t s);
+cudaError_t bucket_merge_prepare();   // opts the kernel into its shared memory
 
 struct CompactArgs {
     void *table;

@@ -30,6 +30,10 @@ D4E_ERR_UNSUPPORTED = -4
 D4E_ERR_STATE = -5
 D4E_KEEP_LEVELS = 1
 D4E_AUTOTUNE = 2
+D4E_DEDUP_DIRECT = 4
+D4E_DEDUP_PARTITIONED = 8
+_DEDUP_FLAGS = {None: 0, "auto": 0, "direct": D4E_DEDUP_DIRECT,
+                "partitioned": D4E_DEDUP_PARTITIONED}
 D4E_BATCH_SEQUENTIAL = 1
 
 _u64p = C.POINTER(C.c_uint64)
@@ -77,6 +81,9 @@ class Stats(C.Structure):
         ("tuned_load", C.c_double),
         ("compact_slots", C.c_uint64),
         ("phase_ms", C.c_double * 6),
+        ("partitioned", C.c_uint64),
+        ("partition_fallbacks", C.c_uint64),
+        ("merge_ms", C.c_double),
     ]
 
     def as_dict(self) -> dict:
@@ -298,7 +305,7 @@ class CudaSearcher:
 
     def __init__(self, frow: Frow, empty_area: Optional[int] = None,
                  rows: Optional[Sequence[int]] = None, keep_levels: bool = False,
-                 autotune: bool = False):
+                 autotune: bool = False, dedup: Optional[str] = None):
         self._frow = frow
         self._h = C.c_void_p()
         if empty_area is not None:
@@ -313,7 +320,8 @@ class CudaSearcher:
             self.rows = list(rows)
             self.width = frow.width
             r = _arr(C.c_uint8, self.rows)
-            flags = (D4E_KEEP_LEVELS if keep_levels else 0) | (D4E_AUTOTUNE if autotune else 0)
+            flags = ((D4E_KEEP_LEVELS if keep_levels else 0) | (D4E_AUTOTUNE if autotune else 0)
+                     | _DEDUP_FLAGS[dedup])
             _check(_lib.d4e_searcher_create_board(frow._h, len(self.rows), r, flags,
                                                   C.byref(self._h)))
         self.height = len(self.rows)
@@ -414,7 +422,7 @@ D4E_BATCH_AUTOTUNE = 4
 
 def batch_run(problems, mode: int = MODE_COUNT, sequential: bool = False, device: int = 0,
               memory_budget: int = 0, max_states: int = 0, beam: int = 0,
-              wide_keys: bool = False, autotune: bool = False):
+              wide_keys: bool = False, autotune: bool = False, dedup: Optional[str] = None):
     """Runs a batch through d4e_batch_run; returns (results, stats dict).
     Each result is a dict (status, count, found, rows, latency_ms, and for a
     found solve-one tiling height x width "grid" (types) and "steps")."""
@@ -422,7 +430,7 @@ def batch_run(problems, mode: int = MODE_COUNT, sequential: bool = False, device
     n = len(problems)
     res = (Result * max(n, 1))()
     flags = ((D4E_BATCH_SEQUENTIAL if sequential else 0) | (D4E_BATCH_WIDE_KEYS if wide_keys else 0)
-             | (D4E_BATCH_AUTOTUNE if autotune else 0))
+             | (D4E_BATCH_AUTOTUNE if autotune else 0) | (_DEDUP_FLAGS[dedup] << 1))
     o = BatchOpts(mode, flags, device, 0, memory_budget, max_states, beam)
     st = Stats()
     _check(_lib.d4e_batch_run(arr, n, C.byref(o), res, C.byref(st)))

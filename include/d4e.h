@@ -101,6 +101,10 @@ typedef struct d4e_searcher d4e_searcher;
 #define D4E_KEEP_LEVELS 1u   /* retain every row's frontier: enables d4e_searcher_solutions */
 #define D4E_AUTOTUNE 2u      /* measure launch plans on the first row of 2^21..2^25 states
                                 (cached per process); replaces KSizing::optimize */
+#define D4E_DEDUP_DIRECT 4u  /* de-duplicate every row by direct hash-table inserts */
+#define D4E_DEDUP_PARTITIONED 8u  /* de-duplicate every eligible row (packed keys, after
+                                     the first row) through hash buckets merged on chip
+                                     (default: direct inserts) */
 
 /* Forgets every launch plan measured so far in this process (the next
  * autotuned engine measures again). */
@@ -188,6 +192,9 @@ typedef struct d4e_stats {
     double phase_ms[6];         /* host wall time inside row steps: selecting instances,
                                    preparing tables, waiting for k_expand, bookkeeping,
                                    waiting for k_compact, row tail */
+    uint64_t partitioned;       /* row groups de-duplicated through buckets */
+    uint64_t partition_fallbacks; /* ... redone with the direct table (bucket overflow) */
+    double merge_ms;            /* device time of k_bucket_merge (also in compact_ms) */
 } d4e_stats;
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st);
@@ -218,6 +225,8 @@ typedef struct d4e_instance {
 #define D4E_BATCH_SEQUENTIAL 1u /* one puzzle at a time, one launch sequence per puzzle */
 #define D4E_BATCH_WIDE_KEYS 2u  /* d4e_batch_run: the general 128-bit key encoding for all */
 #define D4E_BATCH_AUTOTUNE 4u   /* d4e_batch_run: measure launch plans (see D4E_AUTOTUNE) */
+#define D4E_BATCH_DEDUP_DIRECT 8u        /* see D4E_DEDUP_DIRECT */
+#define D4E_BATCH_DEDUP_PARTITIONED 16u  /* see D4E_DEDUP_PARTITIONED */
 
 /* Counts the tilings of every instance.  Default: all instances advance
  * together, one k_expand + one k_compact launch per board row for the whole
