@@ -79,6 +79,7 @@ struct InstDesc {
     uint32_t fwords;
     uint32_t f0_off[kMaxWidth];
     uint32_t f1_off[kMaxWidth];
+    uint32_t f2_off[kMaxWidth];   // row-2 filter of column c, pattern = window row 2
     TypeField types[kMaxTypes];
     uint8_t rows[kMaxHeight];      // board rows, bit c = cell to cover
 };

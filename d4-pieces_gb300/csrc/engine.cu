@@ -313,6 +313,7 @@ uint32_t Engine::add(const InstanceSpec &sp) {
     for (int c = 0; c < kMaxWidth; c++) {
         d.f0_off[c] = in.lib.f0_off[c];
         d.f1_off[c] = in.lib.f1_off[c];
+        d.f2_off[c] = in.lib.f2_off[c];
     }
     filt_total_ += in.lib.filters.size();
     d.n_types = (uint32_t)in.lib.fields.size();

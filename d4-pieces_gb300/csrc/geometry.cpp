@@ -240,8 +240,8 @@ std::string build_piece_lib(const uint64_t *shapes, const uint32_t *counts, uint
 
     // Candidate filters: for column c, bitsets over its placements of those
     // whose row-0 cells fit a row-0 pattern (indexed by the bits right of c;
-    // c itself is always empty at that point) and of those whose row-1 cells
-    // fit a row-1 pattern.
+    // c itself is always empty at that point), and of those whose row-1
+    // (row-2) cells fit a row-1 (row-2) pattern.
     uint32_t maxlen = 1;
     for (uint32_t col = 0; col < width; col++)
         maxlen = std::max<uint32_t>(maxlen, out.col_len[col]);
@@ -260,14 +260,19 @@ std::string build_piece_lib(const uint64_t *shapes, const uint32_t *counts, uint
                     out.filters[out.f0_off[col] + (size_t)p * FW + i / 64] |= 1ull << (i % 64);
             }
         }
-        out.f1_off[col] = (uint32_t)out.filters.size();
-        out.filters.resize(out.filters.size() + ((size_t)1 << width) * FW, 0ull);
-        for (uint32_t q = 0; q < (1u << width); q++)
-            for (uint32_t i = 0; i < out.col_len[col]; i++) {
-                const uint64_t m1 = (out.plc[out.col_off[col] + i].mask >> width) & rowmask;
-                if (!(m1 & ~(uint64_t)q))
-                    out.filters[out.f1_off[col] + (size_t)q * FW + i / 64] |= 1ull << (i % 64);
-            }
+        // Rows 1 and 2: placements whose cells in that row fit its pattern.
+        for (uint32_t r = 1; r <= 2; r++) {
+            uint32_t &off = r == 1 ? out.f1_off[col] : out.f2_off[col];
+            off = (uint32_t)out.filters.size();
+            out.filters.resize(out.filters.size() + ((size_t)1 << width) * FW, 0ull);
+            for (uint32_t q = 0; q < (1u << width); q++)
+                for (uint32_t i = 0; i < out.col_len[col]; i++) {
+                    const uint64_t mr =
+                        (out.plc[out.col_off[col] + i].mask >> (r * width)) & rowmask;
+                    if (!(mr & ~(uint64_t)q))
+                        out.filters[off + (size_t)q * FW + i / 64] |= 1ull << (i % 64);
+                }
+        }
     }
     return {};
 }

@@ -49,6 +49,7 @@ struct PieceLib {
     uint32_t fwords = 1;
     uint32_t f0_off[kMaxWidth] = {};
     uint32_t f1_off[kMaxWidth] = {};
+    uint32_t f2_off[kMaxWidth] = {};
     std::vector<uint64_t> filters;
 };
 

@@ -587,17 +587,20 @@ k_expand(ExpandArgs a) {
                 pop = true;
             } else {
                 const uint32_t c = __ffs(row) - 1;
-                // Next candidate >= idx whose row-0 and row-1 cells fit:
-                // AND of the column's two filter bitsets.
+                // Next candidate >= idx whose row-0, row-1 and row-2 cells
+                // fit: AND of the column's three filter bitsets.
                 const uint32_t fw = d->fwords;
+                const unsigned long long *fb = a.filt + d->filt_off;
                 const unsigned long long *f0 =
-                    a.filt + d->filt_off + d->f0_off[c] + (unsigned long long)(row >> (c + 1)) * fw;
+                    fb + d->f0_off[c] + (unsigned long long)(row >> (c + 1)) * fw;
                 const unsigned long long *f1 =
-                    a.filt + d->filt_off + d->f1_off[c] +
-                    (unsigned long long)((uint32_t)(w >> W) & rowmask) * fw;
+                    fb + d->f1_off[c] + (unsigned long long)((uint32_t)(w >> W) & rowmask) * fw;
+                const unsigned long long *f2 =
+                    fb + d->f2_off[c] +
+                    (unsigned long long)((uint32_t)(w >> (2 * W)) & rowmask) * fw;
                 bool found = false;
                 for (uint32_t k = idx >> 6; k < fw; ++k) {
-                    unsigned long long m = __ldg(f0 + k) & __ldg(f1 + k);
+                    unsigned long long m = __ldg(f0 + k) & __ldg(f1 + k) & __ldg(f2 + k);
                     if (k == (idx >> 6))
                         m &= ~0ull << (idx & 63u);
                     if (m) {

@@ -130,6 +130,7 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
         for (int c = 0; c < kMaxWidth; c++) {
             d.f0_off[c] = lib.f0_off[c];
             d.f1_off[c] = lib.f1_off[c];
+            d.f2_off[c] = lib.f2_off[c];
         }
         d.n_types = (uint32_t)lib.fields.size();
         d.dyn_bits = lib.dyn_bits;
