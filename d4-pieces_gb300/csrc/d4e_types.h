@@ -43,7 +43,7 @@ constexpr uint64_t kUsedMask128 = (1ull << kInstShift128) - 1;
 struct Plc {
     uint64_t mask;
     uint32_t type;
-    uint32_t pad;
+    uint32_t next_type;   // column-relative index of the first placement of the next type
 };
 
 // Copy counter of one piece type: field mask and capacity (count << offset),

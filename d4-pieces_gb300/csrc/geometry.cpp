@@ -236,6 +236,13 @@ std::string build_piece_lib(const uint64_t *shapes, const uint32_t *counts, uint
         if (len > (size_t)kMaxPlcPerCol)
             return "more than 255 placements anchored at one column";
         out.col_len[col] = (uint16_t)len;
+        // A column's placements come grouped by type: each records where its
+        // type's run ends, so a type without copies left is skipped at once.
+        for (size_t i = len; i-- > 0;) {
+            Plc &p = out.plc[out.col_off[col] + i];
+            const bool last = i + 1 == len || out.plc[out.col_off[col] + i + 1].type != p.type;
+            p.next_type = last ? (uint32_t)(i + 1) : out.plc[out.col_off[col] + i + 1].next_type;
+        }
     }
 
     // Candidate filters: for column c, bitsets over its placements of those

@@ -611,19 +611,18 @@ k_expand(ExpandArgs a) {
                 }
                 if (found) {
                     const Plc p = plc[d->col_off[c] + idx];
-                    bool take = !(p.mask & ~w);
-                    TypeField f;
-                    if (take) {
-                        f = d->types[p.type];
-                        take = (u & f.fm) < f.cap;
-                    }
-                    if (take) {
-                        sidx |= (unsigned long long)idx << (8 * depth);
-                        scol |= c << (4 * depth);
-                        ++depth;
-                        w &= ~p.mask;
-                        u += f.fm & (0ull - f.fm);
-                        idx = 0;
+                    if (!(p.mask & ~w)) {
+                        const TypeField f = d->types[p.type];
+                        if ((u & f.fm) < f.cap) {
+                            sidx |= (unsigned long long)idx << (8 * depth);
+                            scol |= c << (4 * depth);
+                            ++depth;
+                            w &= ~p.mask;
+                            u += f.fm & (0ull - f.fm);
+                            idx = 0;
+                        } else {
+                            idx = p.next_type;   // no copies left: skip the type's run
+                        }
                     } else {
                         ++idx;
                     }
