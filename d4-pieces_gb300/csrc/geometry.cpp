@@ -255,11 +255,18 @@ std::string build_piece_lib(const uint64_t *shapes, const uint32_t *counts, uint
     out.fwords = (maxlen + 63) / 64;
     const uint32_t FW = out.fwords;
     const uint64_t rowmask = (1ull << width) - 1ull;
+    // Fixed layout, so that the kernel computes offsets instead of loading
+    // them: row-0 filters of column c at (c * 2^(W-1) + p) * FW, then the
+    // row-1 filters at (W * 2^(W-1) + c * 2^W + q) * FW, then the row-2
+    // filters W * 2^W * FW further on.
+    const size_t n0 = (size_t)1 << (width - 1), n1 = (size_t)1 << width;
+    out.filters.assign((width * n0 + 2 * width * n1) * FW, 0ull);
     for (uint32_t col = 0; col < width; col++) {
-        const uint32_t n0 = 1u << (width - 1 - col);
-        out.f0_off[col] = (uint32_t)out.filters.size();
-        out.filters.resize(out.filters.size() + (size_t)n0 * FW, 0ull);
-        for (uint32_t p = 0; p < n0; p++) {
+        out.f0_off[col] = (uint32_t)((col * n0) * FW);
+        out.f1_off[col] = (uint32_t)((width * n0 + col * n1) * FW);
+        out.f2_off[col] = (uint32_t)((width * n0 + width * n1 + col * n1) * FW);
+        const uint32_t np = 1u << (width - 1 - col);
+        for (uint32_t p = 0; p < np; p++) {
             const uint64_t row0 = ((uint64_t)p << (col + 1)) | (1ull << col);
             for (uint32_t i = 0; i < out.col_len[col]; i++) {
                 const uint64_t m0 = out.plc[out.col_off[col] + i].mask & rowmask;
@@ -269,9 +276,7 @@ std::string build_piece_lib(const uint64_t *shapes, const uint32_t *counts, uint
         }
         // Rows 1 and 2: placements whose cells in that row fit its pattern.
         for (uint32_t r = 1; r <= 2; r++) {
-            uint32_t &off = r == 1 ? out.f1_off[col] : out.f2_off[col];
-            off = (uint32_t)out.filters.size();
-            out.filters.resize(out.filters.size() + ((size_t)1 << width) * FW, 0ull);
+            const uint32_t off = r == 1 ? out.f1_off[col] : out.f2_off[col];
             for (uint32_t q = 0; q < (1u << width); q++)
                 for (uint32_t i = 0; i < out.col_len[col]; i++) {
                     const uint64_t mr =

@@ -589,15 +589,18 @@ k_expand(ExpandArgs a) {
                 const uint32_t c = __ffs(row) - 1;
                 // Next candidate >= idx whose row-0, row-1 and row-2 cells
                 // fit: AND of the column's three filter bitsets.
+                // Fixed filter layout (see build_piece_lib): offsets from
+                // the column and the row patterns, no per-column loads.
                 const uint32_t fw = d->fwords;
                 const unsigned long long *fb = a.filt + d->filt_off;
+                const uint32_t n0 = 1u << (W - 1);
                 const unsigned long long *f0 =
-                    fb + d->f0_off[c] + (unsigned long long)(row >> (c + 1)) * fw;
+                    fb + (unsigned long long)((c << (W - 1)) + (row >> (c + 1))) * fw;
                 const unsigned long long *f1 =
-                    fb + d->f1_off[c] + (unsigned long long)((uint32_t)(w >> W) & rowmask) * fw;
+                    fb + (unsigned long long)(W * n0 + (c << W) + ((uint32_t)(w >> W) & rowmask)) * fw;
                 const unsigned long long *f2 =
-                    fb + d->f2_off[c] +
-                    (unsigned long long)((uint32_t)(w >> (2 * W)) & rowmask) * fw;
+                    fb + (unsigned long long)(W * n0 + (W << W) + (c << W) +
+                                              ((uint32_t)(w >> (2 * W)) & rowmask)) * fw;
                 bool found = false;
                 for (uint32_t k = idx >> 6; k < fw; ++k) {
                     unsigned long long m = __ldg(f0 + k) & __ldg(f1 + k) & __ldg(f2 + k);
