@@ -48,7 +48,7 @@ def parse_args():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--seed", type=int, default=SINGLE_LARGE_SEED)
     ap.add_argument("--workload", choices=("single_large", "medium", "batched", "batched_one",
-                                           "serve"),
+                                           "serve", "family"),
                     default="single_large",
                     help="medium = 8x10 board, 78 cells, 16 pieces (profiling case: frontier "
                          "of ~18M states, a few hundred MB -- larger than L2, a few GB at most)")
@@ -487,6 +487,57 @@ def bench_batched(args, dist: Dist) -> None:
         }), flush=True)
 
 
+FAMILY_TEXT = ("aaaaaaaa\naaaaaaaa\naaaaaaaa\naaabcaaa\n"
+               "aaadaaaa\naaaaaaaa\naaaaaaaa\naaaaaaaa\n")
+
+
+def bench_family(args, dist: Dist) -> None:
+    """Board family (the reference's Board<8> + AtomicCount research run):
+    8x8 with three fixed holes near the centre (regions b, c, d) and one
+    roaming hole (region a: 61 configurations of 60 cells); pieces are the
+    free tetrominoes and pentominoes, each at most once.  Every configuration
+    is one instance of a piece-set batch; the result is the ledger of Naming
+    ranks.  Plain = the same configurations one at a time."""
+    from d4gb import engine as E
+    from d4gb import family as F
+    from d4gb.problem import pentomino_ring
+
+    fam = F.BoardFamily.from_text(FAMILY_TEXT)
+    E.batch_run([pentomino_ring(E.catalogue(5))], device=dist.local_rank)  # context warm-up
+    res, runs = {}, {}
+    for arm, seq in (("batched", False), ("plain", True)):
+        t0 = time.perf_counter()
+        run = F.family_ledger(fam, 4, 5, 0, 64, device=dist.local_rank,
+                              max_states=args.max_states, sequential=seq)
+        wall = time.perf_counter() - t0
+        runs[arm] = run
+        st = run.stats
+        res[arm] = {"wall_s": wall, "configs_per_s": fam.count / wall,
+                    "states_per_s": st["states_out"] / wall, "states": st["states_out"],
+                    "expand_launches": st["expand_launches"],
+                    "expand_ms": st["expand_ms"], "compact_ms": st["compact_ms"]}
+    if runs["batched"].ledger != runs["plain"].ledger:
+        raise RuntimeError("batched and plain ledgers differ")
+    run = runs["batched"]
+    if dist.rank == 0:
+        print(json.dumps({
+            "metric": "configurations/s (board family, piece-set ledger)",
+            "value": res["batched"]["configs_per_s"],
+            "unit": "configurations/s",
+            "n_gpus": dist.world,
+            "config": {"workload": "board family 8x8, 3 fixed + 1 roaming hole (61 "
+                                   "configurations), free tetrominoes + pentominoes at most "
+                                   "once each, Naming ranks over 4-5 cells",
+                       "naming_size": run.naming.size()},
+            "batched": res["batched"], "plain": res["plain"],
+            "speedup_vs_plain": res["batched"]["configs_per_s"] / res["plain"]["configs_per_s"],
+            "ledger_entries": len(run.ledger),
+            "tiled_configs": sum(1 for v in run.per_config.values() if v),
+            "tilings": sum(t for v in run.per_config.values() for _, t in v),
+            "cpu_baseline": None,
+        }), flush=True)
+
+
 SERVE_SEED = 4242
 
 
@@ -604,6 +655,8 @@ def main() -> None:
             bench_batched(args, dist)
         elif args.workload == "serve":
             bench_serve(args, dist)
+        elif args.workload == "family":
+            bench_family(args, dist)
         else:
             bench_ours(args, dist)
     finally:

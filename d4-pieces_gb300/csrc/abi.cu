@@ -442,7 +442,9 @@ d4e::InstanceSpec to_spec(const d4e_instance &in, uint32_t mode, uint64_t max_st
     sp.counts = in.counts;
     sp.n_pieces = in.n_pieces;
     sp.sym = in.sym;
-    sp.mode = mode == D4E_MODE_SOLVE_ONE ? d4e::Mode::SolveOne : d4e::Mode::Count;
+    sp.mode = mode == D4E_MODE_SOLVE_ONE ? d4e::Mode::SolveOne
+              : mode == D4E_MODE_SETS    ? d4e::Mode::Sets
+                                         : d4e::Mode::Count;
     sp.max_states = max_states;
     sp.beam = beam;
     return sp;
@@ -478,6 +480,8 @@ void engine_result(Engine &eng, uint32_t id, uint32_t mode, d4e_result *r) {
         r->count = r->found;
     } else {
         r->count = eng.count(id);
+        if (mode == D4E_MODE_SETS)
+            r->found = (uint32_t)eng.sets(id).size();
     }
 }
 
@@ -487,20 +491,32 @@ extern "C" {
 
 void d4e_autotune_clear(void) { d4e::autotune_clear(); }
 
-int d4e_batch_run(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
-                  d4e_result *results, d4e_stats *st) {
+}  // extern "C"
+
+namespace {
+
+// The batch runner behind d4e_batch_run and d4e_batch_sets; `sets`
+// receives each instance's piece multisets in Sets mode.
+int batch_impl(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
+               d4e_result *results, d4e_stats *st,
+               std::vector<std::vector<d4e::PieceSet>> *sets) {
     return guarded([&] {
         if ((!insts && n) || (!results && n))
             return fail(D4E_ERR_INVALID, "null pointer");
         const d4e_batch_opts o = opts ? *opts : d4e_batch_opts{};
-        if (o.mode > D4E_MODE_SOLVE_ONE)
+        if (o.mode > D4E_MODE_SETS)
             return fail(D4E_ERR_INVALID, "unknown mode");
         for (uint32_t i = 0; i < n; i++)
-            if (insts[i].width * insts[i].height > sizeof(results[i].grid) && o.mode)
+            if (insts[i].width * insts[i].height > sizeof(results[i].grid) &&
+                o.mode == D4E_MODE_SOLVE_ONE)
                 return fail(D4E_ERR_INVALID, "solve-one boards are limited to 512 cells");
+        if (sets)
+            sets->assign(n, {});
         const auto t0 = std::chrono::steady_clock::now();
         auto finish = [&](d4e::Engine &eng, uint32_t id, uint32_t i) {
             d4e::engine_result(eng, id, o.mode, &results[i]);
+            if (sets && results[i].status == 0)
+                (*sets)[i] = eng.sets(id);
             results[i].tag = i;
             results[i].queued_ms = 0;
             results[i].latency_ms =
@@ -572,6 +588,54 @@ int d4e_batch_run(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *o
             if (st)
                 fill_stats(eng, st, true);
         }
+        return D4E_OK;
+    });
+}
+
+}  // namespace
+
+extern "C" {
+
+int d4e_batch_run(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
+                  d4e_result *results, d4e_stats *st) {
+    return batch_impl(insts, n, opts, results, st, nullptr);
+}
+
+int d4e_batch_sets(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
+                   d4e_result *results, uint64_t *set_offsets, uint8_t *set_copies,
+                   uint64_t *set_tilings, uint64_t max_sets, d4e_stats *st) {
+    std::vector<std::vector<d4e::PieceSet>> sets;
+    d4e_batch_opts o = opts ? *opts : d4e_batch_opts{};
+    o.mode = D4E_MODE_SETS;
+    if (n && !set_offsets)
+        return fail(D4E_ERR_INVALID, "null pointer");
+    for (uint32_t i = 0; i < n; i++)
+        if (insts && insts[i].n_pieces > D4E_SET_PIECES)
+            return fail(D4E_ERR_INVALID, "piece-set mode takes at most 64 piece types");
+    const int rc = batch_impl(insts, n, &o, results, st, &sets);
+    if (rc != D4E_OK)
+        return rc;
+    return guarded([&] {
+        uint64_t total = 0;
+        for (uint32_t i = 0; i < n; i++) {
+            set_offsets[i] = total;
+            total += sets[i].size();
+        }
+        set_offsets[n] = total;
+        if (total > max_sets)
+            return fail(D4E_ERR_INVALID, "max_sets too small: " + std::to_string(total) +
+                                             " piece sets (set_offsets[n])");
+        if (total && (!set_copies || !set_tilings))
+            return fail(D4E_ERR_INVALID, "null pointer");
+        uint64_t k = 0;
+        for (uint32_t i = 0; i < n; i++)
+            for (const d4e::PieceSet &ps : sets[i]) {
+                std::memset(set_copies + k * D4E_SET_PIECES, 0, D4E_SET_PIECES);
+                std::memcpy(set_copies + k * D4E_SET_PIECES, ps.copies.data(),
+                            std::min<size_t>(ps.copies.size(), D4E_SET_PIECES));
+                set_tilings[k] = ps.tilings;
+                k++;
+            }
         return D4E_OK;
     });
 }

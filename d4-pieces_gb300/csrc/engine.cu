@@ -1260,6 +1260,49 @@ StepStats Engine::step_impl() {
             }
             continue;
         }
+        if (in.mode == Mode::Sets && in.row == in.height && in.seg_len) {
+            // The final row's states are the tiling piece multisets: read
+            // them back and decode each used-copy counter per piece type.
+            std::vector<ulonglong2> rec(in.seg_len);
+            std::vector<unsigned long long> cn;
+            cuda_check(cudaMemcpyAsync(rec.data(), keys_[nxt].p + begin,
+                                       in.seg_len * sizeof(ulonglong2), cudaMemcpyDeviceToHost,
+                                       stream_),
+                       "read final states");
+            if (!k64_) {
+                cn.resize(in.seg_len);
+                cuda_check(cudaMemcpyAsync(cn.data(), cnts_[nxt].p + begin,
+                                           in.seg_len * sizeof(unsigned long long),
+                                           cudaMemcpyDeviceToHost, stream_),
+                           "read final states");
+            }
+            cuda_check(cudaStreamSynchronize(stream_), "read final states");
+            tot_.d2h_bytes += in.seg_len * (k64_ ? 16 : 24);
+            const unsigned long long usedmask =
+                in.lib.used_bits ? ((1ull << in.lib.used_bits) - 1ull) : 0ull;
+            in.sets.clear();
+            unsigned long long sum = 0;
+            for (uint64_t k = 0; k < in.seg_len; k++) {
+                const unsigned long long used =
+                    k64_ ? (rec[k].x >> in.lib.dyn_bits) & usedmask : rec[k].y & kUsedMask128;
+                PieceSet ps;
+                ps.tilings = k64_ ? rec[k].y : cn[k];
+                for (const TypeField &f : in.lib.fields)
+                    ps.copies.push_back(
+                        f.fm ? (uint8_t)((used & f.fm) >> __builtin_ctzll(f.fm)) : 0);
+                sum += ps.tilings;
+                in.sets.push_back(std::move(ps));
+            }
+            std::sort(in.sets.begin(), in.sets.end(),
+                      [](const PieceSet &a, const PieceSet &b) { return a.copies < b.copies; });
+            in.active = false;
+            in.done = true;
+            n_active_--;
+            in.result = sum;
+            in.result_ready = true;
+            in.seg_len = 0;
+            continue;
+        }
         if (in.row == in.height || in.seg_len == 0) {
             in.active = false;
             in.done = true;

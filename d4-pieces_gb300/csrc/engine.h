@@ -119,7 +119,16 @@ struct Tuning {
     double load = 0.5;               // hash table load factor aimed at
 };
 
-enum class Mode : uint32_t { Count = 0, SolveOne = 1 };
+// Count: tilings.  SolveOne: one tiling.  Sets: the piece multisets that
+// tile the board (the final row's used-copy counters), each with its number
+// of tilings.
+enum class Mode : uint32_t { Count = 0, SolveOne = 1, Sets = 2 };
+
+// One piece multiset of a Sets instance: copies per input piece type.
+struct PieceSet {
+    std::vector<uint8_t> copies;
+    uint64_t tilings = 0;
+};
 
 struct InstanceSpec {
     uint32_t width = 8;
@@ -211,6 +220,8 @@ public:
     // Solve-one result: true and the tiling (row-major type grid, step grid,
     // width * height cells each, -1 = not covered) when one exists.
     bool solution(uint32_t id, int8_t *type_grid, int16_t *step_grid);
+    // Sets-mode result (valid once done).
+    const std::vector<PieceSet> &sets(uint32_t id) const { return inst_.at(id).sets; }
     // Frees a finished instance's id for reuse by a later add().
     void release(uint32_t id);
     const std::vector<uint64_t> &level_sizes(uint32_t id) const { return inst_.at(id).level_sizes; }
@@ -256,6 +267,7 @@ private:
         bool sampled = false;
         std::vector<LevelRef> levels;
         bool found = false;
+        std::vector<PieceSet> sets;   // Sets mode result
         std::vector<int8_t> tgrid;
         std::vector<int16_t> sgrid;
     };

@@ -221,6 +221,8 @@ _sig("d4e_batch_count", C.c_int, C.POINTER(Instance), C.c_uint32, C.c_uint32, C.
      C.POINTER(Stats))
 _sig("d4e_batch_run", C.c_int, C.POINTER(Instance), C.c_uint32, C.POINTER(BatchOpts),
      C.POINTER(Result), C.POINTER(Stats))
+_sig("d4e_batch_sets", C.c_int, C.POINTER(Instance), C.c_uint32, C.POINTER(BatchOpts),
+     C.POINTER(Result), _u64p, _u8p, _u64p, C.c_uint64, C.POINTER(Stats))
 _sig("d4e_server_create", C.c_int, C.POINTER(ServerOpts), C.POINTER(C.c_void_p))
 _sig("d4e_server_submit", C.c_int, C.c_void_p, C.POINTER(Instance), C.c_uint32, C.c_uint64)
 _sig("d4e_server_poll", C.c_int, C.c_void_p, C.POINTER(Result), C.c_uint32, _u32p)
@@ -436,6 +438,44 @@ def batch_run(problems, mode: int = MODE_COUNT, sequential: bool = False, device
     _check(_lib.d4e_batch_run(arr, n, C.byref(o), res, C.byref(st)))
     return ([res[i].as_dict(problems[i].width, problems[i].height) for i in range(n)],
             st.as_dict())
+
+
+MODE_SETS = 2
+SET_PIECES = 64
+
+
+def batch_sets(problems, device: int = 0, memory_budget: int = 0, max_states: int = 0,
+               sequential: bool = False, wide_keys: bool = False, max_sets: int = 1 << 14):
+    """Piece-set mode (d4e_batch_sets): for each problem, the piece multisets
+    that tile its board (the problem's counts are maxima), as a list of
+    (copies per piece, tilings) sorted by copies; plus the results and stats.
+    When the batch has more than max_sets sets it runs once more with room
+    for the number the first run reported."""
+    arr, keep = _instances(problems)
+    n = len(problems)
+    res = (Result * max(n, 1))()
+    flags = (D4E_BATCH_SEQUENTIAL if sequential else 0) | (D4E_BATCH_WIDE_KEYS if wide_keys else 0)
+    o = BatchOpts(MODE_SETS, flags, device, 0, memory_budget, max_states, 0)
+    offs = (C.c_uint64 * (n + 1))()
+    st = Stats()
+    while True:
+        copies = (C.c_uint8 * max(max_sets * SET_PIECES, 1))()
+        til = (C.c_uint64 * max(max_sets, 1))()
+        rc = _lib.d4e_batch_sets(arr, n, C.byref(o), res, offs, copies, til, max_sets,
+                                 C.byref(st))
+        if rc == D4E_ERR_INVALID and offs[n] > max_sets:
+            max_sets = offs[n]
+            continue
+        _check(rc)
+        break
+    out = []
+    for i, p in enumerate(problems):
+        sets = []
+        for k in range(offs[i], offs[i + 1]):
+            row = bytes(copies[k * SET_PIECES:(k + 1) * SET_PIECES])[: len(p.shapes)]
+            sets.append((tuple(row), til[k]))
+        out.append(sets)
+    return out, [res[i].as_dict() for i in range(n)], st.as_dict()
 
 
 def autotune_clear() -> None:

@@ -237,6 +237,9 @@ int d4e_batch_count(const d4e_instance *insts, uint32_t n, uint32_t flags, int32
 
 #define D4E_MODE_COUNT 0u      /* solve-all: count every tiling */
 #define D4E_MODE_SOLVE_ONE 1u  /* one tiling, or none when there is none */
+#define D4E_MODE_SETS 2u       /* the piece multisets that tile the board (the pieces'
+                                  counts are maxima), each with its number of tilings;
+                                  results: count = all tilings, found = number of sets */
 
 typedef struct d4e_batch_opts {
     uint32_t mode;              /* D4E_MODE_* for every instance */
@@ -280,6 +283,19 @@ typedef struct d4e_result {
  * whether the instance runs alone or in any batch.  results[i].tag = i. */
 int d4e_batch_run(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
                   d4e_result *results, d4e_stats *st);
+
+/* Piece-set mode over a batch (the reference's research use: which piece
+ * combinations tile each board of a family, src/search.cpp:25-54, with the
+ * ledger of Naming ranks, src/naming.inl:6-72, left to the caller).  Every
+ * instance runs in D4E_MODE_SETS; its multisets are set_offsets[i] ..
+ * set_offsets[i+1]-1, sorted by copies; set k has set_copies[k * 64 + p]
+ * copies of piece p and set_tilings[k] tilings.  set_offsets has n + 1
+ * entries; when more than max_sets sets exist the call fails with
+ * D4E_ERR_INVALID and set_offsets[n] holds the number needed. */
+#define D4E_SET_PIECES 64u
+int d4e_batch_sets(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
+                   d4e_result *results, uint64_t *set_offsets, uint8_t *set_copies,
+                   uint64_t *set_tilings, uint64_t max_sets, d4e_stats *st);
 
 /* ------------------------------------------------------------------------
  * Serving: a request loop on a native worker thread.  No counterpart in the

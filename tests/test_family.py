@@ -1,0 +1,99 @@
+"""Board-family text parsing, configuration enumeration and combination
+ranks (host logic, no GPU).
+
+Parsing follows the reference's Shape / Board text rules
+(src/Shape.hpp:49-77, src/board.hpp:15-38); ranks follow its Naming
+(src/naming.cpp:34-90, src/naming.inl:6-72) and are checked here as a
+bijection onto 0..size-1 whose size matches a brute-force count."""
+import itertools
+
+from d4gb import family as F
+
+
+def test_shape_text_rules():
+    assert F.parse_shape("#.#\n.#.") == 0b101 | (0b010 << 8)
+    # a leading newline is skipped; '*', '1', '@', '#', 'X', '%' are cells;
+    # ' ', '0', '.', '-', '_' are holes; anything else is ignored
+    assert F.parse_shape("\n*1@#X%") == 0b111111
+    assert F.parse_shape(" 0.-_#") == 1 << 5
+    assert F.parse_shape("#?!#") == 0b11
+    # a row longer than the width runs on into the next row's bits
+    assert F.parse_shape("#########") == (1 << 9) - 1
+    assert F.parse_shape("#\n#", width=11) == 1 | (1 << 11)
+
+
+def test_board_regions_and_configs():
+    fam = F.BoardFamily.from_text("\naaab....\naaab....\nccdd....\nccdd....\n")
+    assert fam.names == ["a", "b", "c", "d"]
+    assert fam.base == 0x0F0F0F0F
+    assert fam.regions == [0x707, 0x808, 0x3030000, 0xC0C0000]
+    assert fam.count == 6 * 2 * 4 * 4 == 192
+    assert fam.left == 12
+    cfgs = list(fam.configs())
+    assert len(cfgs) == len(set(cfgs)) == 192
+    for m in cfgs:
+        assert m & ~fam.base == 0
+        for r in fam.regions:
+            assert bin(r & ~m).count("1") == 1
+
+
+def test_base_marks_belong_to_every_region():
+    # as in the reference, a non-letter cell mark is kept in every region's
+    # text, so it belongs to each region as well as to the base
+    fam = F.BoardFamily.from_text("a#\nb#")
+    assert fam.base == 0b11 | (0b11 << 8)
+    assert fam.regions == [0b11 | (0b10 << 8), 0b10 | (0b11 << 8)]
+    cfgs = list(fam.configs())
+    assert len(cfgs) == fam.count == 9
+    # picking the shared cell twice leaves three cells, not two
+    assert (0b11 | (0b11 << 8)) & ~(0b10) in cfgs
+
+
+def test_board_problem_rows():
+    p = F.board_problem(0x0F0F0F0F, [0b11], [6])
+    assert (p.width, p.height, p.rows) == (8, 4, [15, 15, 15, 15])
+    q = F.board_problem(1 | (1 << 11), [0b1], [2], width=11)
+    assert (q.width, q.height, q.rows) == (11, 2, [1, 1])
+
+
+def brute_force(min_m, max_m, min_n, max_n, tgt, sizes):
+    pieces = [(m, i) for m in range(min_m, max_m + 1) for i in range(sizes.get(m, 0))]
+    out = []
+    for r in range(min_n, max_n + 1):
+        for c in itertools.combinations(pieces, r):
+            if sum(m for m, _ in c) == tgt:
+                out.append(c)
+    return out
+
+
+def test_naming_is_a_bijection():
+    # the example in the reference's Naming self-test: sizes 2, 4, 5 with
+    # 3, 7 and 6 pieces, 2..8 pieces covering 20 cells
+    sizes = {2: 3, 4: 7, 5: 6}
+    nm = F.Naming(2, 5, 2, 8, 20, sizes)
+    combos = brute_force(2, 5, 2, 8, 20, sizes)
+    assert nm.size() == len(combos) == 1191
+    seen = set()
+    for c in combos:
+        chosen = [[i for m, i in c if m == mm] for mm in range(2, 6)]
+        r = nm.name(chosen)
+        assert r is not None and 0 <= r < nm.size()
+        seen.add(r)
+        assert nm.resolve(r) == [sorted(x) for x in chosen]
+    assert len(seen) == nm.size()
+
+
+def test_naming_order():
+    # profiles (pieces per size) in lexicographic order; within one profile
+    # the smallest size is the most significant digit and each digit is the
+    # lexicographic rank of the chosen subset
+    nm = F.Naming(1, 2, 0, 9, 3, {1: 3, 2: 2})
+    assert nm.profiles == [(1, 1), (3, 0)]
+    got = [nm.resolve(i) for i in range(nm.size())]
+    assert got == [[[0], [0]], [[0], [1]], [[1], [0]], [[1], [1]], [[2], [0]], [[2], [1]],
+                   [[0, 1, 2], []]]
+    assert nm.name([[0], [0, 1]]) is None          # 5 cells, not 3
+    assert nm.resolve(nm.size()) is None
+    # piece-count limits
+    assert F.Naming(1, 2, 2, 2, 3, {1: 3, 2: 2}).size() == 6
+    assert F.Naming(1, 2, 3, 3, 3, {1: 3, 2: 2}).size() == 1

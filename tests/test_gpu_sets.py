@@ -1,0 +1,144 @@
+"""Piece-set mode (d4e_batch_sets) and the board-family driver.
+
+A piece set is the multiset of copies a tiling uses; the engine keeps the
+final row's states, whose copy counters are exactly those multisets.  Every
+reported set is checked against the oracle: its number of tilings equals the
+oracle's count with that set as the piece counts, and on the small families
+the whole list equals the oracle's exhaustive search over all multisets.
+The sum over a board's sets equals its counting-mode result (the
+reference's golden counts)."""
+import itertools
+import json
+
+import pytest
+
+from conftest import GOLDEN, case_problem, load_cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = [c for c in load_cases() if c["width"] <= 8]
+FAMILY = "\naaab....\naaab....\nccdd....\nccdd....\n"
+
+
+@pytest.fixture(scope="module")
+def E(engine):
+    if engine.device_count() == 0:
+        pytest.fail("no CUDA device visible")
+    return engine
+
+
+@pytest.fixture(scope="module")
+def free():
+    raw = json.loads((GOLDEN / "catalogue.json").read_text())
+    return {int(m): v for m, v in raw["free"].items()}
+
+
+def oracle_sets(oracle, p, area_only=None):
+    """Every multiset within p.counts (covering area_only cells, when given)
+    with a non-zero oracle count, in the engine's order (sorted copies)."""
+    areas = [bin(v).count("1") for v in p.shapes]
+    cells = p.cells if area_only is None else area_only
+    out = []
+    for copies in itertools.product(*[range(k + 1) for k in p.counts]):
+        if sum(a * k for a, k in zip(areas, copies)) != cells:
+            continue
+        q = type(p)(p.width, p.height, p.rows, p.shapes, list(copies), p.sym)
+        n = oracle.solve_count(q)
+        if n:
+            out.append((tuple(copies), n))
+    return sorted(out)
+
+
+def test_ring_is_one_set(E):
+    ring = next(c for c in CASES if c["name"].startswith("pentomino ring"))
+    sets, res, st = E.batch_sets([case_problem(ring)])
+    assert res[0]["status"] == 0
+    assert res[0]["found"] == 1 and res[0]["count"] == 520
+    assert sets == [[((1,) * 12, 520)]]
+
+
+@pytest.mark.parametrize("wide", [False, True])
+def test_golden_cases_sets_sum_to_counts(E, oracle, wide):
+    probs = [case_problem(c) for c in CASES]
+    sets, res, _ = E.batch_sets(probs, wide_keys=wide)
+    for c, p, s, r in zip(CASES, probs, sets, res):
+        assert r["status"] == 0, c["name"]
+        assert sum(t for _, t in s) == c["count"] == r["count"], c["name"]
+        assert r["found"] == len(s)
+        assert [x for x, _ in s] == sorted(x for x, _ in s)
+        areas = [bin(v).count("1") for v in p.shapes]
+        for copies, t in s:
+            assert t > 0
+            assert all(0 <= k <= m for k, m in zip(copies, p.counts)), c["name"]
+            assert sum(a * k for a, k in zip(areas, copies)) == p.cells, c["name"]
+            if c["count"] < 10 ** 6:
+                q = type(p)(p.width, p.height, p.rows, p.shapes, list(copies), p.sym)
+                assert oracle.solve_count(q) == t, (c["name"], copies)
+
+
+SMALL = [c for c in CASES if 0 < c["count"] < 10 ** 6 and
+         sum(1 for _ in itertools.product(*[range(k + 1) for k in c["counts"]])) <= 4096]
+
+
+@pytest.mark.parametrize("case", SMALL, ids=[c["name"] for c in SMALL])
+def test_sets_equal_exhaustive_oracle(E, oracle, case):
+    p = case_problem(case)
+    sets, res, _ = E.batch_sets([p])
+    assert sets[0] == oracle_sets(oracle, p)
+
+
+def test_alone_and_batched_identical(E):
+    probs = [case_problem(c) for c in CASES]
+    a, _, _ = E.batch_sets(probs, sequential=True)
+    b, _, _ = E.batch_sets(probs)
+    assert a == b
+
+
+def test_max_sets_retry(E):
+    probs = [case_problem(c) for c in CASES]
+    full, _, _ = E.batch_sets(probs)
+    small, _, _ = E.batch_sets(probs, max_sets=1)
+    assert small == full
+
+
+@pytest.mark.parametrize("copies", [1, 2])
+def test_family_matches_exhaustive_oracle(E, oracle, free, copies):
+    from d4gb import family as F
+
+    fam = F.BoardFamily.from_text(FAMILY)
+    shapes = free[2] + free[3] + free[4]
+    per_config, ledger = F.tiling_sets(fam, shapes, [copies] * len(shapes))
+    assert set(per_config) == set(fam.configs())
+    want_ledger = {}
+    for m in fam.configs():
+        p = F.board_problem(m, shapes, [copies] * len(shapes))
+        want = oracle_sets(oracle, p, fam.left)
+        assert per_config[m] == want, hex(m)
+        assert sum(t for _, t in want) == oracle.solve_count(p)
+        for c, _ in want:
+            want_ledger[c] = want_ledger.get(c, 0) + 1
+    assert ledger == want_ledger
+
+
+@pytest.mark.parametrize("rotations_only", [False, True])
+def test_family_ledger_ranks(E, oracle, rotations_only):
+    """The AtomicCount ledger: Naming rank -> configurations tiled."""
+    from d4gb import family as F
+
+    fam = F.BoardFamily.from_text(FAMILY)
+    run = F.family_ledger(fam, 2, 4, 3, 5, rotations_only=rotations_only)
+    sym = 0b01101001 if rotations_only else 0xFF
+    want = {}
+    for m in fam.configs():
+        for r in range(run.naming.size()):
+            chosen = run.naming.resolve(r)
+            if not 3 <= sum(len(x) for x in chosen) <= 5:
+                continue
+            counts = []
+            for d, x in enumerate(chosen):
+                counts += [1 if i in x else 0 for i in range(run.naming.sizes[2 + d])]
+            p = F.board_problem(m, run.shapes, counts, sym)
+            if oracle.solve_count(p):
+                want[r] = want.get(r, 0) + 1
+    assert run.ledger == want
+    assert run.unsolved(fam) == [m for m in fam.configs() if not run.per_config[m]]
