@@ -491,6 +491,8 @@ extern "C" {
 
 void d4e_autotune_clear(void) { d4e::autotune_clear(); }
 
+void d4e_release_cached_memory(void) { d4e::release_idle_pools(); }
+
 }  // extern "C"
 
 namespace {
@@ -499,7 +501,7 @@ namespace {
 // receives each instance's piece multisets in Sets mode.
 int batch_impl(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
                d4e_result *results, d4e_stats *st,
-               std::vector<std::vector<d4e::PieceSet>> *sets) {
+               std::vector<d4e::PieceSets> *sets) {
     return guarded([&] {
         if ((!insts && n) || (!results && n))
             return fail(D4E_ERR_INVALID, "null pointer");
@@ -604,7 +606,7 @@ int d4e_batch_run(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *o
 int d4e_batch_sets(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
                    d4e_result *results, uint64_t *set_offsets, uint8_t *set_copies,
                    uint64_t *set_tilings, uint64_t max_sets, d4e_stats *st) {
-    std::vector<std::vector<d4e::PieceSet>> sets;
+    std::vector<d4e::PieceSets> sets;
     d4e_batch_opts o = opts ? *opts : d4e_batch_opts{};
     o.mode = D4E_MODE_SETS;
     if (n && !set_offsets)
@@ -628,14 +630,16 @@ int d4e_batch_sets(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *
         if (total && (!set_copies || !set_tilings))
             return fail(D4E_ERR_INVALID, "null pointer");
         uint64_t k = 0;
-        for (uint32_t i = 0; i < n; i++)
-            for (const d4e::PieceSet &ps : sets[i]) {
+        for (uint32_t i = 0; i < n; i++) {
+            const d4e::PieceSets &ps = sets[i];
+            const size_t nt = std::min<size_t>(ps.n_types, D4E_SET_PIECES);
+            for (size_t j = 0; j < ps.size(); j++, k++) {
                 std::memset(set_copies + k * D4E_SET_PIECES, 0, D4E_SET_PIECES);
-                std::memcpy(set_copies + k * D4E_SET_PIECES, ps.copies.data(),
-                            std::min<size_t>(ps.copies.size(), D4E_SET_PIECES));
-                set_tilings[k] = ps.tilings;
-                k++;
+                std::memcpy(set_copies + k * D4E_SET_PIECES, ps.copies.data() + j * ps.n_types,
+                            nt);
+                set_tilings[k] = ps.tilings[j];
             }
+        }
         return D4E_OK;
     });
 }

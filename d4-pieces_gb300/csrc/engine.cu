@@ -24,6 +24,53 @@ void cuda_check(cudaError_t e, const char *what) {
 
 namespace {
 thread_local cudaMemPool_t *tl_pool_ref = nullptr;
+
+// Idle engine pools, at most one per device: an engine that ends hands its
+// pool (with the device memory it has mapped) to the next engine created on
+// that device, so back-to-back batches do not map their memory again.
+std::mutex g_pool_mu;
+std::vector<std::pair<int, cudaMemPool_t>> g_idle_pools;
+
+cudaMemPool_t take_idle_pool(int device) {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    for (size_t i = 0; i < g_idle_pools.size(); i++)
+        if (g_idle_pools[i].first == device) {
+            const cudaMemPool_t p = g_idle_pools[i].second;
+            g_idle_pools.erase(g_idle_pools.begin() + i);
+            return p;
+        }
+    return nullptr;
+}
+
+void give_idle_pool(int device, cudaMemPool_t pool) {
+    {
+        std::lock_guard<std::mutex> lk(g_pool_mu);
+        bool have = false;
+        for (auto &e : g_idle_pools)
+            have |= e.first == device;
+        if (!have) {
+            g_idle_pools.emplace_back(device, pool);
+            return;
+        }
+    }
+    cudaMemPoolDestroy(pool);
+}
+}  // namespace
+
+void release_idle_pools() {
+    std::vector<std::pair<int, cudaMemPool_t>> pools;
+    {
+        std::lock_guard<std::mutex> lk(g_pool_mu);
+        pools.swap(g_idle_pools);
+    }
+    for (auto &e : pools) {
+        int prev = -1;
+        cudaGetDevice(&prev);
+        cudaSetDevice(e.first);
+        cudaMemPoolDestroy(e.second);
+        if (prev >= 0)
+            cudaSetDevice(prev);
+    }
 }
 
 cudaError_t engine_malloc_async(void **p, size_t bytes, cudaStream_t s) {
@@ -160,7 +207,8 @@ Engine::Engine(const EngineOpts &opts) : opts_(opts) {
     EngineScope g(opts_.device, &pool_);
     cuda_check(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, opts_.device),
                "cudaDeviceGetAttribute");
-    {
+    pool_ = take_idle_pool(opts_.device);
+    if (!pool_) {
         // The engine's own pool; freed blocks stay in it for the next
         // growth instead of going back to the driver at every sync.
         cudaMemPoolProps props{};
@@ -252,7 +300,7 @@ Engine::~Engine() {
         cudaStreamDestroy(stream_);
     }
     if (pool_)
-        cudaMemPoolDestroy(pool_);
+        give_idle_pool(opts_.device, pool_);
 }
 
 void Engine::ensure_inst_capacity(size_t n) {
@@ -750,8 +798,11 @@ StepStats Engine::step_impl() {
         // Small frontiers (fewer states than a quarter of the resident lanes)
         // are split: each state's walk is cut by its first placement into
         // `fan` work items (the longest placement list of a column), so a
-        // handful of states still fills the GPU.  Larger ones already do, and
-        // warps fetch chunks independently with in-warp work donation.
+        // handful of states still fills the GPU; when even that leaves most
+        // lanes idle (a first row: one state whose fills run to ~1e6) by
+        // its first two placements, fan^2 items.  Larger frontiers already
+        // fill the GPU, and warps fetch chunks independently with in-warp
+        // work donation.
         uint32_t fan = 0;
         if (n_grp * 4 < slots * 256)
             for (uint32_t id : grp)
@@ -759,7 +810,8 @@ StepStats Engine::step_impl() {
                     fan = std::max<uint32_t>(fan, inst_[id].desc.col_len[c]);
         if (fan <= 1)
             fan = 0;
-        const uint64_t per = fan ? fan : 1;
+        const bool fan2 = fan && n_grp * fan * 4 < slots * 256;
+        const uint64_t per = fan ? (fan2 ? (uint64_t)fan * fan : fan) : 1;
         const uint64_t items = n_grp * per;
         // Launch plan: warps take chunks independently, about
         // `chunks_per_warp` chunks per resident warp, within [32, chunk_cap]
@@ -890,6 +942,7 @@ StepStats Engine::step_impl() {
             a.n_chunks = n_chunks;
             a.chunk_states = chunk;
             a.fan = fan;
+            a.fan2 = fan2;
             a.insts = insts_.p;
             a.plc = plc_.p;
             a.filt = filt_.p;
@@ -983,6 +1036,7 @@ StepStats Engine::step_impl() {
         a.n_chunks = n_chunks;
         a.chunk_states = chunk;
         a.fan = fan;
+        a.fan2 = fan2;
         a.insts = insts_.p;
         a.plc = plc_.p;
         a.filt = filt_.p;
@@ -1280,21 +1334,39 @@ StepStats Engine::step_impl() {
             tot_.d2h_bytes += in.seg_len * (k64_ ? 16 : 24);
             const unsigned long long usedmask =
                 in.lib.used_bits ? ((1ull << in.lib.used_bits) - 1ull) : 0ull;
-            in.sets.clear();
+            // Sort key: the copy counters repacked type-major (type 0 most
+            // significant), so numeric order is the lexicographic order of
+            // the copies; the counters take used_bits <= 40 bits in all.
+            const auto &fields = in.lib.fields;
+            const size_t nt = fields.size();
+            std::vector<std::pair<unsigned long long, unsigned long long>> ks(in.seg_len);
             unsigned long long sum = 0;
             for (uint64_t k = 0; k < in.seg_len; k++) {
                 const unsigned long long used =
                     k64_ ? (rec[k].x >> in.lib.dyn_bits) & usedmask : rec[k].y & kUsedMask128;
-                PieceSet ps;
-                ps.tilings = k64_ ? rec[k].y : cn[k];
-                for (const TypeField &f : in.lib.fields)
-                    ps.copies.push_back(
-                        f.fm ? (uint8_t)((used & f.fm) >> __builtin_ctzll(f.fm)) : 0);
-                sum += ps.tilings;
-                in.sets.push_back(std::move(ps));
+                unsigned long long key = 0;
+                for (const TypeField &f : fields)
+                    if (f.fm)
+                        key = (key << __builtin_popcountll(f.fm)) |
+                              ((used & f.fm) >> __builtin_ctzll(f.fm));
+                ks[k] = {key, k64_ ? rec[k].y : cn[k]};
+                sum += ks[k].second;
             }
-            std::sort(in.sets.begin(), in.sets.end(),
-                      [](const PieceSet &a, const PieceSet &b) { return a.copies < b.copies; });
+            std::sort(ks.begin(), ks.end());
+            PieceSets &out = in.sets;
+            out.n_types = (uint32_t)nt;
+            out.copies.assign(in.seg_len * nt, 0);
+            out.tilings.resize(in.seg_len);
+            for (uint64_t k = 0; k < in.seg_len; k++) {
+                unsigned long long key = ks[k].first;
+                for (size_t t = nt; t-- > 0;)
+                    if (fields[t].fm) {
+                        const int b = __builtin_popcountll(fields[t].fm);
+                        out.copies[k * nt + t] = (uint8_t)(key & ((1ull << b) - 1ull));
+                        key >>= b;
+                    }
+                out.tilings[k] = ks[k].second;
+            }
             in.active = false;
             in.done = true;
             n_active_--;

@@ -72,6 +72,9 @@ void autotune_clear();
 // Device bytes an allocation can still get: free memory plus what the
 // device's stream-ordered pools hold in reserve.
 size_t device_available_bytes(int device, size_t *total);
+// Destroys the idle engine pools (the device memory they keep for the next
+// engine goes back to the driver).
+void release_idle_pools();
 
 enum class KeyMode { Auto, K64, K128 };
 
@@ -125,9 +128,14 @@ struct Tuning {
 enum class Mode : uint32_t { Count = 0, SolveOne = 1, Sets = 2 };
 
 // One piece multiset of a Sets instance: copies per input piece type.
-struct PieceSet {
+// Piece multisets of a Sets-mode instance: set k uses copies[k * n_types + t]
+// copies of piece type t and has tilings[k] tilings; sets are in
+// lexicographic order of their copies.
+struct PieceSets {
+    uint32_t n_types = 0;
     std::vector<uint8_t> copies;
-    uint64_t tilings = 0;
+    std::vector<uint64_t> tilings;
+    size_t size() const { return tilings.size(); }
 };
 
 struct InstanceSpec {
@@ -221,7 +229,7 @@ public:
     // width * height cells each, -1 = not covered) when one exists.
     bool solution(uint32_t id, int8_t *type_grid, int16_t *step_grid);
     // Sets-mode result (valid once done).
-    const std::vector<PieceSet> &sets(uint32_t id) const { return inst_.at(id).sets; }
+    const PieceSets &sets(uint32_t id) const { return inst_.at(id).sets; }
     // Frees a finished instance's id for reuse by a later add().
     void release(uint32_t id);
     const std::vector<uint64_t> &level_sizes(uint32_t id) const { return inst_.at(id).level_sizes; }
@@ -267,7 +275,7 @@ private:
         bool sampled = false;
         std::vector<LevelRef> levels;
         bool found = false;
-        std::vector<PieceSet> sets;   // Sets mode result
+        PieceSets sets;   // Sets mode result
         std::vector<int8_t> tgrid;
         std::vector<int16_t> sgrid;
     };

@@ -382,6 +382,7 @@ k_expand(ExpandArgs a) {
     WarpStage &ws = stage[threadIdx.x >> 5];
     const unsigned lt_mask = (1u << lane) - 1u;
     const uint32_t fan = a.fan ? a.fan : 1u;
+    const uint32_t per = a.fan2 ? fan * fan : fan;   // work items per state
     unsigned long long raw = 0;
 
     // Warp-uniform chunk cursor.
@@ -457,7 +458,7 @@ k_expand(ExpandArgs a) {
                 dyn_bits = d->dyn_bits;
                 dynmask = (1ull << dyn_bits) - 1ull;
                 usedmask = (1ull << d->used_bits) - 1ull;
-                const unsigned long long si = item / fan;
+                const unsigned long long si = item / per;
                 const ulonglong2 rec = a.recs[si];
                 wit = (d->flags & kInstWitness) != 0u;
                 if constexpr (K64) {
@@ -476,13 +477,21 @@ k_expand(ExpandArgs a) {
                 min_depth = 0;
                 active = true;
                 if (a.fan) {
-                    // Place this item's first choice at the root, then walk
-                    // only beneath it (min_depth = 1).
-                    const uint32_t choice = (uint32_t)(item % fan);
-                    const uint32_t row = (uint32_t)w & rowmask;
-                    if (row == 0) {
-                        active = choice == 0;   // complete row: one item emits it
-                    } else {
+                    // Place this item's first choice (and, split two ways,
+                    // its second) and walk only beneath them: min_depth =
+                    // the placements fixed.  Items whose choices do not fit
+                    // are empty; a row completed early is emitted by the one
+                    // item whose remaining choices are 0.
+                    const uint32_t rem = (uint32_t)(item % per);
+                    uint32_t choice = rem % fan;
+                    uint32_t later = rem / fan;   // choices below the current level
+                    active = true;
+                    for (uint32_t lv = 0; active && lv < (a.fan2 ? 2u : 1u); ++lv) {
+                        const uint32_t row = (uint32_t)w & rowmask;
+                        if (row == 0) {
+                            active = choice == 0 && later == 0;
+                            break;
+                        }
                         const uint32_t c = __ffs(row) - 1;
                         active = false;
                         if (choice < d->col_len[c]) {
@@ -490,16 +499,18 @@ k_expand(ExpandArgs a) {
                             if (!(p.mask & ~w)) {
                                 const TypeField f = d->types[p.type];
                                 if ((u & f.fm) < f.cap) {
-                                    sidx = choice;
-                                    scol = c;
-                                    depth = 1;
+                                    sidx |= (unsigned long long)choice << (8 * depth);
+                                    scol |= c << (4 * depth);
+                                    ++depth;
                                     w &= ~p.mask;
                                     u += f.fm & (0ull - f.fm);
                                     active = true;
-                                    min_depth = 1;
+                                    min_depth = depth;
                                 }
                             }
                         }
+                        choice = later;
+                        later = 0;
                     }
                 }
                 rw = w;

@@ -222,7 +222,8 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
             sg.tbase = 0;
             sg.tcap = L.cap_slots;
             const uint32_t fan = n * 4 < slots * 256 && fan_max > 1 ? fan_max : 0;
-            const uint64_t items = n * (fan ? fan : 1);
+            const bool fan2 = fan && n * fan * 4 < slots * 256;
+            const uint64_t items = n * (fan ? (fan2 ? (uint64_t)fan * fan : fan) : 1);
             const uint64_t warps = slots * 8;
             uint64_t chunk = (items + 8 * warps - 1) / (8 * warps);
             chunk = std::min<uint64_t>(std::max<uint64_t>((chunk + 31) / 32 * 32, 32), 1024);
@@ -240,6 +241,7 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
             a.n_chunks = n_chunks;
             a.chunk_states = chunk;
             a.fan = fan;
+            a.fan2 = fan2;
             a.insts = d_desc;
             a.plc = d_plc;
             a.filt = d_filt;

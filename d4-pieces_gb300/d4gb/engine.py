@@ -230,6 +230,7 @@ _sig("d4e_server_drain", C.c_int, C.c_void_p, C.c_double)
 _sig("d4e_server_stats_get", C.c_int, C.c_void_p, C.POINTER(ServerStats))
 _sig("d4e_server_destroy", None, C.c_void_p)
 _sig("d4e_autotune_clear", None)
+_sig("d4e_release_cached_memory", None)
 _sig("d4e_canonical_grid", C.c_int, C.c_uint32, C.c_uint32, _u8p, _i8p, _i8p)
 _sig("d4e_count_noalloc", C.c_int, C.POINTER(Instance), C.c_void_p, _u64p, _u64p)
 
@@ -445,42 +446,54 @@ SET_PIECES = 64
 
 
 def batch_sets(problems, device: int = 0, memory_budget: int = 0, max_states: int = 0,
-               sequential: bool = False, wide_keys: bool = False, max_sets: int = 1 << 14):
+               sequential: bool = False, wide_keys: bool = False, max_sets: int = 1 << 22,
+               arrays: bool = False):
     """Piece-set mode (d4e_batch_sets): for each problem, the piece multisets
     that tile its board (the problem's counts are maxima), as a list of
     (copies per piece, tilings) sorted by copies; plus the results and stats.
-    When the batch has more than max_sets sets it runs once more with room
-    for the number the first run reported."""
+    The output buffers are allocated untouched (pages are only mapped where
+    sets are written); when the batch has more than max_sets sets it runs
+    once more with room for the number the first run reported.  arrays=True
+    returns (offsets[n + 1], copies[sets, 64], tilings[sets]) numpy arrays in
+    place of the per-problem lists."""
     arr, keep = _instances(problems)
     n = len(problems)
     res = (Result * max(n, 1))()
     flags = (D4E_BATCH_SEQUENTIAL if sequential else 0) | (D4E_BATCH_WIDE_KEYS if wide_keys else 0)
     o = BatchOpts(MODE_SETS, flags, device, 0, memory_budget, max_states, 0)
-    offs = (C.c_uint64 * (n + 1))()
+    offs = np.zeros(n + 1, dtype=np.uint64)
     st = Stats()
     while True:
-        copies = (C.c_uint8 * max(max_sets * SET_PIECES, 1))()
-        til = (C.c_uint64 * max(max_sets, 1))()
-        rc = _lib.d4e_batch_sets(arr, n, C.byref(o), res, offs, copies, til, max_sets,
-                                 C.byref(st))
-        if rc == D4E_ERR_INVALID and offs[n] > max_sets:
-            max_sets = offs[n]
+        copies = np.empty((max(max_sets, 1), SET_PIECES), dtype=np.uint8)
+        til = np.empty(max(max_sets, 1), dtype=np.uint64)
+        rc = _lib.d4e_batch_sets(arr, n, C.byref(o), res, offs.ctypes.data_as(_u64p),
+                                 copies.ctypes.data_as(_u8p), til.ctypes.data_as(_u64p),
+                                 max_sets, C.byref(st))
+        if rc == D4E_ERR_INVALID and int(offs[n]) > max_sets:
+            max_sets = int(offs[n])
             continue
         _check(rc)
         break
+    if arrays:
+        total = int(offs[n])
+        out = (offs, copies[:total], til[:total])
+        return out, [res[i].as_dict() for i in range(n)], st.as_dict()
     out = []
     for i, p in enumerate(problems):
-        sets = []
-        for k in range(offs[i], offs[i + 1]):
-            row = bytes(copies[k * SET_PIECES:(k + 1) * SET_PIECES])[: len(p.shapes)]
-            sets.append((tuple(row), til[k]))
-        out.append(sets)
+        a, b = int(offs[i]), int(offs[i + 1])
+        rows = map(tuple, copies[a:b, : len(p.shapes)].tolist())
+        out.append(list(zip(rows, til[a:b].tolist())))
     return out, [res[i].as_dict() for i in range(n)], st.as_dict()
 
 
 def autotune_clear() -> None:
     """Forgets the launch plans measured so far in this process."""
     _lib.d4e_autotune_clear()
+
+
+def release_cached_memory() -> None:
+    """Returns the device memory kept for the next engine to the driver."""
+    _lib.d4e_release_cached_memory()
 
 
 class Server:

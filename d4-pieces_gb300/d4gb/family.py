@@ -22,6 +22,8 @@ import math
 from dataclasses import dataclass, field
 from typing import Dict, Iterator, List, Sequence, Tuple
 
+import numpy as np
+
 from .problem import Problem
 
 _CELL = set("*1@#X%")
@@ -233,6 +235,74 @@ def _comb_unrank(nm: int, k: int, n: int) -> List[int]:
 SetList = List[Tuple[Tuple[int, ...], int]]
 
 
+@dataclass
+class FamilySets:
+    """Kept piece sets of a family run, as arrays: the distinct boards
+    (`masks`), each board's sets in rows offsets[i]..offsets[i+1]-1 of
+    `copies` (copies per piece) and `tilings`, and `mult[i]`, how many of
+    the family's configurations are board i."""
+    masks: List[int]
+    mult: np.ndarray
+    offsets: np.ndarray
+    copies: np.ndarray
+    tilings: np.ndarray
+    stats: dict
+
+    def per_config(self) -> Dict[int, SetList]:
+        out = {}
+        for i, m in enumerate(self.masks):
+            a, b = int(self.offsets[i]), int(self.offsets[i + 1])
+            out[m] = list(zip(map(tuple, self.copies[a:b].tolist()),
+                              self.tilings[a:b].tolist()))
+        return out
+
+    def ledger(self) -> Tuple[np.ndarray, np.ndarray]:
+        """(distinct sets, configurations each tiles): every board's sets
+        are distinct, so a set's count is the sum of its boards' mult."""
+        if not len(self.copies):
+            return self.copies, np.zeros(0, np.int64)
+        k = self.copies.shape[1]
+        rows = np.ascontiguousarray(self.copies).view(np.dtype((np.void, k))).ravel()
+        uniq, inv = np.unique(rows, return_inverse=True)
+        per_row = np.repeat(self.mult, np.diff(self.offsets).astype(np.int64))
+        n = np.bincount(inv.ravel(), weights=per_row, minlength=len(uniq)).astype(np.int64)
+        return uniq.view(np.uint8).reshape(-1, k), n
+
+
+def family_sets(family: BoardFamily, shapes: Sequence[int], counts: Sequence[int] | None = None,
+                sym: int = 0xFF, min_n: int = 0, max_n: int = 1 << 30, device: int = 0,
+                max_states: int = 0, sequential: bool = False) -> FamilySets:
+    """Every configuration of the family in one piece-set batch; keeps the
+    sets of min_n..max_n pieces covering `left` cells (the combinations the
+    reference ranks).  Overlapping regions can map two picks to one board:
+    each distinct board is solved once and counted with its multiplicity;
+    a board that kept more cells (a cell cleared twice) has no kept set."""
+    from . import engine as E
+
+    counts = list(counts) if counts is not None else [1] * len(shapes)
+    areas = np.array([bin(v).count("1") for v in shapes], np.int64)
+    mult_of: Dict[int, int] = {}
+    for m in family.configs():
+        mult_of[m] = mult_of.get(m, 0) + 1
+    uniq = sorted(mult_of)
+    probs = [board_problem(m, shapes, counts, sym, width=family.width) for m in uniq]
+    (offs, copies, tilings), results, st = E.batch_sets(
+        probs, device=device, max_states=max_states, sequential=sequential, arrays=True)
+    for m, r in zip(uniq, results):
+        if r["status"] != 0:
+            raise E.D4Error(r["status"], f"configuration {m:#x} failed")
+    k = len(shapes)
+    c = copies[:, :k]
+    wide = c.astype(np.int64)
+    n_pieces = wide.sum(axis=1)
+    keep = (n_pieces >= min_n) & (n_pieces <= max_n) & (wide @ areas == family.left)
+    board = np.repeat(np.arange(len(uniq)), np.diff(offs).astype(np.int64))
+    kept_offs = np.zeros(len(uniq) + 1, np.int64)
+    np.cumsum(np.bincount(board[keep], minlength=len(uniq)), out=kept_offs[1:])
+    return FamilySets(uniq, np.array([mult_of[m] for m in uniq], np.int64), kept_offs,
+                      np.ascontiguousarray(c[keep]), tilings[keep], st)
+
+
 def tiling_sets(family: BoardFamily, shapes: Sequence[int], counts: Sequence[int] | None = None,
                 sym: int = 0xFF, min_n: int = 0, max_n: int = 1 << 30, device: int = 0,
                 max_states: int = 0, sequential: bool = False, stats: dict | None = None,
@@ -245,47 +315,34 @@ def tiling_sets(family: BoardFamily, shapes: Sequence[int], counts: Sequence[int
     AtomicCount ledger, keyed by the multiset instead of its rank).
     sequential runs the boards one at a time; stats receives the batch's
     engine counters."""
-    from . import engine as E
-
-    counts = list(counts) if counts is not None else [1] * len(shapes)
-    areas = [bin(v).count("1") for v in shapes]
-    masks = list(family.configs())
-    # Overlapping regions can map two picks to one board: solve each once.
-    # Only combinations covering exactly `left` cells are ranked by the
-    # reference, so boards that kept more cells (a cell cleared twice)
-    # report none.
-    uniq = sorted(set(masks))
-    probs = [board_problem(m, shapes, counts, sym, width=family.width) for m in uniq]
-    sets, results, st = E.batch_sets(probs, device=device, max_states=max_states,
-                                     sequential=sequential)
+    fs = family_sets(family, shapes, counts, sym, min_n, max_n, device, max_states, sequential)
     if stats is not None:
-        stats.update(st)
-    found: Dict[int, SetList] = {}
-    for m, st, r in zip(uniq, sets, results):
-        if r["status"] != 0:
-            raise E.D4Error(r["status"], f"configuration {m:#x} failed")
-        found[m] = [(c, t) for c, t in st if min_n <= sum(c) <= max_n
-                    and sum(a * k for a, k in zip(areas, c)) == family.left]
-    per_config = {m: found[m] for m in uniq}
-    ledger: Dict[Tuple[int, ...], int] = {}
-    for m in masks:
-        for copies, _ in found[m]:
-            ledger[copies] = ledger.get(copies, 0) + 1
-    return per_config, ledger
+        stats.update(fs.stats)
+    sets, n = fs.ledger()
+    return fs.per_config(), dict(zip(map(tuple, sets.tolist()), n.tolist()))
 
 
 @dataclass
 class FamilyRun:
     naming: Naming
     shapes: List[int]
-    per_config: Dict[int, SetList]
+    sets: FamilySets
     ledger: Dict[int, int]          # Naming rank -> configurations it tiles
-    stats: dict = field(default_factory=dict)
+
+    @property
+    def stats(self) -> dict:
+        return self.sets.stats
+
+    @property
+    def per_config(self) -> Dict[int, SetList]:
+        return self.sets.per_config()
 
     def unsolved(self, family: BoardFamily) -> List[int]:
         """Configurations no combination tiles (the reference's ZERO-count
         report, src/searcher.cpp:110-115)."""
-        return [m for m in family.configs() if not self.per_config.get(m)]
+        empty = {m for i, m in enumerate(self.sets.masks)
+                 if self.sets.offsets[i] == self.sets.offsets[i + 1]}
+        return [m for m in family.configs() if m in empty]
 
 
 def family_ledger(family: BoardFamily, min_m: int, max_m: int, min_n: int, max_n: int,
@@ -304,20 +361,24 @@ def family_ledger(family: BoardFamily, min_m: int, max_m: int, min_n: int, max_n
     for v in shapes:
         sizes[bin(v).count("1")] += 1
     naming = Naming(min_m, max_m, min_n, max_n, family.left, sizes)
-    stats: dict = {}
-    per_config, by_copies = tiling_sets(family, shapes, None, ROTATIONS if rotations_only else FULL_D4,
-                                        min_n, max_n, device, max_states, sequential, stats)
+    fs = family_sets(family, shapes, None, ROTATIONS if rotations_only else FULL_D4,
+                     min_n, max_n, device, max_states, sequential)
+    sets, counts = fs.ledger()
+    # piece index -> (size digit, index within its size)
+    digit, within, seen = [], [], {m: 0 for m in range(min_m, max_m + 1)}
+    for v in shapes:
+        m = bin(v).count("1")
+        digit.append(m - min_m)
+        within.append(seen[m])
+        seen[m] += 1
     ledger: Dict[int, int] = {}
-    for copies, n in by_copies.items():
+    for row, n in zip(sets.tolist(), counts.tolist()):
         chosen: List[List[int]] = [[] for _ in range(min_m, max_m + 1)]
-        seen = {m: 0 for m in range(min_m, max_m + 1)}
-        for v, k in zip(shapes, copies):
-            m = bin(v).count("1")
+        for p, k in enumerate(row):
             if k:
-                chosen[m - min_m].append(seen[m])
-            seen[m] += 1
+                chosen[digit[p]].append(within[p])
         rank = naming.name(chosen)
         if rank is None:
-            raise ValueError(f"combination {copies} has no Naming rank")
+            raise ValueError(f"combination {row} has no Naming rank")
         ledger[rank] = n
-    return FamilyRun(naming, shapes, per_config, ledger, stats)
+    return FamilyRun(naming, shapes, fs, ledger)

@@ -110,6 +110,13 @@ typedef struct d4e_searcher d4e_searcher;
  * autotuned engine measures again). */
 void d4e_autotune_clear(void);
 
+/* Device memory kept for reuse: when an engine (a searcher, a batch call, a
+ * server lane) ends, its memory pool, with the device memory it has mapped,
+ * is kept for the next engine on that device (at most one pool per device),
+ * so back-to-back calls do not map their memory again.  This call returns
+ * the kept memory to the driver. */
+void d4e_release_cached_memory(void);
+
 /* CudaSearcher(uint64_t empty_area): 8-wide board, height = number of rows up
  * to the last cell to cover (src/searcher_cuda.cu:12-21).  The frow tables
  * must have width 8 and have been transferred. */

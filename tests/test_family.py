@@ -97,3 +97,66 @@ def test_naming_order():
     # piece-count limits
     assert F.Naming(1, 2, 2, 2, 3, {1: 3, 2: 2}).size() == 6
     assert F.Naming(1, 2, 3, 3, 3, {1: 3, 2: 2}).size() == 1
+
+
+def fake_batch_sets(oracle):
+    """batch_sets answered by the oracle's exhaustive search (host logic
+    only: the arrays a GPU batch would return)."""
+    import numpy as np
+
+    def run(probs, arrays=False, **kw):
+        assert arrays
+        offs, rows, til = [0], [], []
+        for p in probs:
+            areas = [bin(v).count("1") for v in p.shapes]
+            for copies in itertools.product(*[range(k + 1) for k in p.counts]):
+                if sum(a * k for a, k in zip(areas, copies)) != p.cells:
+                    continue
+                q = type(p)(p.width, p.height, p.rows, p.shapes, list(copies), p.sym)
+                n = oracle.solve_count(q)
+                if n:
+                    rows.append(list(copies) + [0] * (64 - len(copies)))
+                    til.append(n)
+            offs.append(len(rows))
+        out = (np.array(offs, np.uint64), np.array(rows, np.uint8).reshape(-1, 64),
+               np.array(til, np.uint64))
+        return out, [{"status": 0} for _ in probs], {"states_out": 0}
+    return run
+
+
+def test_family_driver_host_logic(monkeypatch, oracle, catalogue_golden):
+    """Filtering by area and piece count, board multiplicity (overlapping
+    regions) and the ledger, with the batch answered by the oracle."""
+    from d4gb import engine as E
+
+    monkeypatch.setattr(E, "batch_sets", fake_batch_sets(oracle))
+    free = catalogue_golden["free"]
+    shapes = free[1] + free[2] + free[3]
+    # 'a' and 'b' share the two '#' cells: picking one twice leaves 5
+    # cells, and picking both (in either order) gives one board twice
+    fam = F.BoardFamily.from_text("aa##\nbb..\n")
+    assert fam.left == 4 and fam.count == 16 and len(set(fam.configs())) == 15
+    per_config, ledger = F.tiling_sets(fam, shapes)
+    areas = [bin(v).count("1") for v in shapes]
+    want = {}
+    for m in fam.configs():
+        p = F.board_problem(m, shapes, [1] * len(shapes))
+        for copies in itertools.product((0, 1), repeat=len(shapes)):
+            if sum(a * k for a, k in zip(areas, copies)) != 4:
+                continue
+            q = F.board_problem(m, shapes, list(copies))
+            if oracle.solve_count(q):
+                want[copies] = want.get(copies, 0) + 1
+        if bin(m).count("1") != 4:
+            assert per_config[m] == []
+    assert ledger == want and max(want.values()) >= 2
+    few, _ = F.tiling_sets(fam, shapes, min_n=3, max_n=3)
+    assert all(sum(c) == 3 for v in few.values() for c, _ in v)
+    run = F.family_ledger(fam, 1, 3, 0, 9)
+    assert sum(run.ledger.values()) == sum(want.values())
+    for r, n in run.ledger.items():
+        chosen = run.naming.resolve(r)
+        copies = tuple(1 if i in chosen[d] else 0
+                       for d, size in enumerate((1, 1, 2)) for i in range(size))
+        assert want[copies] == n
+    assert run.unsolved(fam) == [m for m in fam.configs() if not run.per_config[m]]

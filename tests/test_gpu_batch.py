@@ -117,3 +117,15 @@ def test_frontier_limit_fails_only_that_instance(E):
         else:
             assert r["status"] == 0 and r["count"] == c["count"], c["name"]
     assert st["failed"] == sum(1 for s in sizes if s > limit)
+
+
+def test_kept_memory_reuse_and_release(E):
+    """An ended engine's pool is reused by the next one; releasing it
+    changes no result."""
+    probs = [case_problem(c) for c in SMALL]
+    want = [c["count"] for c in SMALL]
+    for release in (False, False, True, False):
+        if release:
+            E.release_cached_memory()
+        res, _ = E.batch_run(probs)
+        assert [r["count"] for r in res] == want
