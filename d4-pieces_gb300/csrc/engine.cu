@@ -799,10 +799,13 @@ StepStats Engine::step_impl() {
         // are split: each state's walk is cut by its first placement into
         // `fan` work items (the longest placement list of a column), so a
         // handful of states still fills the GPU; when even that leaves most
-        // lanes idle (a first row: one state whose fills run to ~1e6) by
-        // its first two placements, fan^2 items.  Larger frontiers already
-        // fill the GPU, and warps fetch chunks independently with in-warp
-        // work donation.
+        // lanes idle (a first row: one state whose fills run to ~1e6) by its
+        // first two placements, fan^2 items -- unless the step as a whole
+        // is large (16x the resident lanes): then the engine is busy (a
+        // server lane under load) and its small groups, new arrivals mostly,
+        // must not flood the GPU with mostly empty items.  Larger frontiers
+        // already fill the GPU, and warps fetch chunks independently with
+        // in-warp work donation.
         uint32_t fan = 0;
         if (n_grp * 4 < slots * 256)
             for (uint32_t id : grp)
@@ -810,7 +813,8 @@ StepStats Engine::step_impl() {
                     fan = std::max<uint32_t>(fan, inst_[id].desc.col_len[c]);
         if (fan <= 1)
             fan = 0;
-        const bool fan2 = fan && n_grp * fan * 4 < slots * 256;
+        const bool fan2 = fan && opts_.max_split_levels >= 2 &&
+                          n_grp * fan * 4 < slots * 256 && n_cur_ < slots * 256 * 16;
         const uint64_t per = fan ? (fan2 ? (uint64_t)fan * fan : fan) : 1;
         const uint64_t items = n_grp * per;
         // Launch plan: warps take chunks independently, about

@@ -100,6 +100,11 @@ struct EngineOpts {
     // on every SM for kernels of another engine running concurrently.
     int expand_ctas_per_sm = 0;
     bool high_priority = false;    // create the engine's stream at the highest priority
+    // Placements fixed per work item when a frontier is too small to fill
+    // the GPU (1 or 2; see the launch plan).  Two levels fill the whole GPU
+    // from a handful of states, which an engine sharing the GPU with a
+    // latency-critical one should not do.
+    uint32_t max_split_levels = 2;
     // Measure launch plans on the first row of 2^21..2^25 states and keep
     // the fastest (cached per key encoding, board width and device).
     bool autotune = false;
