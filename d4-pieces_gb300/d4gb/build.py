@@ -21,6 +21,7 @@ LIB_DIR = PKG_ROOT / "lib"
 LIB_PATH = LIB_DIR / "libd4e.so"
 HOST_DIR = PKG_ROOT / "host"
 EXAMPLE_PATH = LIB_DIR / "example_step"
+FAMILY_EXAMPLE_PATH = LIB_DIR / "example_family"
 INCLUDE = PKG_ROOT.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -88,25 +89,26 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
-    _build_example(verbose)
+    _build_example("example_step.cpp", EXAMPLE_PATH, ["searcher_cuda.h"], verbose)
+    _build_example("example_family.cpp", FAMILY_EXAMPLE_PATH,
+                   ["searcher_cuda.h", "board_family.h"], verbose)
     return LIB_PATH
 
 
-def _build_example(verbose: bool) -> Path:
-    """The C++ facade's example driver, linked against libd4e.so."""
-    src = HOST_DIR / "example_step.cpp"
-    deps = [src, HOST_DIR / "searcher_cuda.h", INCLUDE / "d4e.h", LIB_PATH]
-    if not _needs_rebuild(EXAMPLE_PATH, deps):
-        return EXAMPLE_PATH
+def _build_example(name: str, out: Path, headers: list[str], verbose: bool) -> Path:
+    """A C++ facade example driver, linked against libd4e.so."""
+    src = HOST_DIR / name
+    deps = [src, INCLUDE / "d4e.h", LIB_PATH] + [HOST_DIR / h for h in headers]
+    if not _needs_rebuild(out, deps):
+        return out
     cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-Wall", "-I", str(HOST_DIR),
-           str(src), "-o", str(EXAMPLE_PATH), "-L", str(LIB_DIR), "-ld4e",
-           "-Wl,-rpath,$ORIGIN"]
+           str(src), "-o", str(out), "-L", str(LIB_DIR), "-ld4e", "-Wl,-rpath,$ORIGIN"]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"example build failed\n{r.stdout}\n{r.stderr}")
-    return EXAMPLE_PATH
+        raise RuntimeError(f"example build failed ({name})\n{r.stdout}\n{r.stderr}")
+    return out
 
 
 if __name__ == "__main__":

@@ -7,6 +7,8 @@ Parsing follows the reference's Shape / Board text rules
 bijection onto 0..size-1 whose size matches a brute-force count."""
 import itertools
 
+import pytest
+
 from d4gb import family as F
 
 
@@ -160,3 +162,59 @@ def test_family_driver_host_logic(monkeypatch, oracle, catalogue_golden):
                        for d, size in enumerate((1, 1, 2)) for i in range(size))
         assert want[copies] == n
     assert run.unsolved(fam) == [m for m in fam.configs() if not run.per_config[m]]
+
+
+@pytest.fixture(scope="module")
+def host_check(tmp_path_factory):
+    """The C++ facade's Board / Naming, compiled alone (no GPU calls)."""
+    import shutil
+    import subprocess
+
+    from conftest import REPO
+
+    out = tmp_path_factory.mktemp("host") / "family_host_check"
+    cxx = shutil.which("g++") or "g++"
+    r = subprocess.run([cxx, "-O1", "-std=c++17", "-Wall", "-Werror",
+                        "-I", str(REPO / "d4-pieces_gb300" / "host"),
+                        str(REPO / "tests" / "family_host_check.cpp"), "-o", str(out)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return out
+
+
+def run_check(exe, *args):
+    import subprocess
+
+    r = subprocess.run([str(exe)] + [str(a) for a in args], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return r.stdout.splitlines()
+
+
+@pytest.mark.parametrize("text", ["\naaab....\naaab....\nccdd....\nccdd....\n",
+                                  "aa##\nbb..\n",
+                                  "aaaaaaaa\naaaaaaaa\naaabaaaa\naaaacaaa\naaaaaaaa\n",
+                                  "\n#%X@*.1\nab-_ 0Z\n"])
+def test_cpp_board_matches_python(host_check, tmp_path, text):
+    f = tmp_path / "board.txt"
+    f.write_text(text)
+    lines = run_check(host_check, "board", f)
+    fam = F.BoardFamily.from_text(text)
+    assert lines[0] == f"base {fam.base:x}"
+    assert lines[1:1 + len(fam.regions)] == [f"region {r:x}" for r in fam.regions]
+    assert lines[1 + len(fam.regions)] == f"count {fam.count} left {fam.left}"
+    assert lines[2 + len(fam.regions):] == [f"config {m:x}" for m in fam.configs()]
+
+
+@pytest.mark.parametrize("args", [(2, 5, 2, 8, 20, 3, 0, 7, 6), (1, 2, 0, 9, 3, 3, 2),
+                                  (3, 5, 0, 64, 37, 2, 5, 12), (4, 5, 3, 11, 40, 5, 12)])
+def test_cpp_naming_matches_python(host_check, args):
+    min_m, max_m, min_n, max_n, tgt, *sizes = args
+    lines = run_check(host_check, "naming", *args)
+    nm = F.Naming(min_m, max_m, min_n, max_n, tgt,
+                  {min_m + d: s for d, s in enumerate(sizes)})
+    assert lines[0] == f"size {nm.size()}"
+    assert lines[-1] == "roundtrip ok"
+    for r, line in enumerate(lines[1:-1]):
+        want = " ".join(f"{min_m + d}:{i}" for d, c in enumerate(nm.resolve(r)) for i in c)
+        assert line == f"rank {r}: {want}".rstrip(), r

@@ -142,3 +142,29 @@ def test_family_ledger_ranks(E, oracle, rotations_only):
                 want[r] = want.get(r, 0) + 1
     assert run.ledger == want
     assert run.unsolved(fam) == [m for m in fam.configs() if not run.per_config[m]]
+
+
+def test_cpp_family_driver_matches_python(E, tmp_path):
+    """The C++ facade's AtomicCount run (example_family) and the Python
+    driver give the same ledger and the same ZERO-count boards."""
+    import subprocess
+
+    from d4gb import build
+    from d4gb import family as F
+
+    text = FAMILY + "\n"
+    f = tmp_path / "family.txt"
+    f.write_text(text)
+    r = subprocess.run([str(build.FAMILY_EXAMPLE_PATH), str(f), "2", "4", "0", "64"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.splitlines()
+    fam = F.BoardFamily.from_text(text)
+    run = F.family_ledger(fam, 2, 4, 0, 64)
+    ranked, total, weighted = (int(x) for x in lines[-1].split()[1:])
+    assert ranked == len(run.ledger)
+    assert total == sum(run.ledger.values())
+    assert weighted == sum((k + 1) * v for k, v in run.ledger.items())
+    zero = [int(x.split()[-1], 16) for x in lines if x.startswith("ZERO-count board")]
+    assert zero == run.unsolved(fam)
+    assert f"number of pieces combinations: {run.naming.size()}" in lines
