@@ -491,6 +491,32 @@ FAMILY_TEXT = "aaaaaaaa\naaaaaaaa\naaabaaaa\naaaacaaa\naaaaaaaa\n"
 FAMILY_MAX_STATES = 1 << 30
 
 
+def family_cpu_baseline(fam, shapes, budget: float) -> tuple[dict, dict]:
+    """The oracle's exact row DP (count mode: the states of the piece-set run,
+    which also reads its final row back) over the family's boards in order
+    until the time budget is spent; returns the baseline and the counts."""
+    from d4gb import family as F
+    from oracle import pyoracle
+
+    pyoracle.build()
+    threads = os.cpu_count() or 1
+    boards = sorted(set(fam.configs()))
+    counts, states = {}, 0
+    t0 = time.perf_counter()
+    for m in boards:
+        p = F.board_problem(m, shapes, [1] * len(shapes))
+        r = pyoracle.rowdp(p, threads=threads)
+        counts[m] = r["count"]
+        states += r["states_total"]
+        if time.perf_counter() - t0 > budget:
+            break
+    el = time.perf_counter() - t0
+    return ({"value": len(counts) / el, "unit": "configurations/s", "cores": threads,
+             "kind": "port", "states_per_s": states / el,
+             "sample": (f"exact row DP (oracle/, count mode) on the first {len(counts)} of "
+                        f"{len(boards)} boards in {el:.1f} s on {threads} threads")}, counts)
+
+
 def bench_family(args, dist: Dist) -> None:
     """Board family (the reference's Board<8> + AtomicCount research run):
     8x5 with two fixed holes (regions b, c) and one roaming hole (region a:
@@ -528,6 +554,17 @@ def bench_family(args, dist: Dist) -> None:
     if runs["batched"].ledger != runs["plain"].ledger:
         raise RuntimeError("batched and plain ledgers differ")
     run = runs["batched"]
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        cpu, counts = family_cpu_baseline(fam, run.shapes, args.cpu_budget)
+        fs = run.sets
+        for i, m in enumerate(fs.masks):
+            if m in counts:
+                got = int(fs.tilings[int(fs.offsets[i]):int(fs.offsets[i + 1])].sum())
+                if got != counts[m]:
+                    raise RuntimeError(f"board {m:#x}: sets sum to {got} tilings, "
+                                       f"the oracle counts {counts[m]}")
+        cpu["checked_boards"] = len(counts)
     if dist.rank == 0:
         print(json.dumps({
             "metric": "configurations/s (board family, piece-set ledger)",
@@ -545,7 +582,7 @@ def bench_family(args, dist: Dist) -> None:
             "tiled_configs": len(run.sets.masks) - len(set(run.unsolved(fam))),
             "sets": int(run.sets.offsets[-1]),
             "tilings": int(run.sets.tilings.sum()),
-            "cpu_baseline": None,
+            "cpu_baseline": cpu,
         }), flush=True)
 
 
