@@ -382,3 +382,25 @@ def family_ledger(family: BoardFamily, min_m: int, max_m: int, min_n: int, max_n
             raise ValueError(f"combination {row} has no Naming rank")
         ledger[rank] = n
     return FamilyRun(naming, shapes, fs, ledger)
+
+
+def read_ledger_file(path, configs: int, names: int, kind: str = "bit"):
+    """Reads a FileBit / FileByte ledger file (the reference's layout,
+    src/search.cpp:56-226; written by the C++ facade's LedgerFile):
+    returns (descriptors[configs, 4] = shape, count, solved ms, padding;
+    tiled[names] = configurations each rank tiles; logged[names, configs]
+    booleans)."""
+    width = configs if kind == "byte" else (configs + 7) // 8
+    raw = np.fromfile(path, dtype=np.uint8)
+    want = configs * 32 + names * 8 + names * width
+    if raw.size != want:
+        raise ValueError(f"ledger file has {raw.size} bytes, this family needs {want}")
+    desc = raw[: configs * 32].view(np.uint64).reshape(configs, 4)
+    tiled = raw[configs * 32: configs * 32 + names * 8].view(np.uint64)
+    led = raw[configs * 32 + names * 8:].reshape(names, width)
+    if kind == "byte":
+        logged = led != 0
+    else:
+        logged = np.unpackbits(led, axis=1, bitorder="little")[:, :configs].astype(bool)
+    return desc, tiled, logged
+

@@ -48,6 +48,50 @@ int main(int argc, char **argv) {
         std::printf("roundtrip ok\n");
         return 0;
     }
-    std::fprintf(stderr, "usage: board <file> | naming <min_m> <max_m> <min_n> <max_n> <tgt> <sizes...>\n");
+    if (argc >= 6 && std::string(argv[1]) == "ledgerfile") {
+        // ledgerfile <path> <configs> <names> <bit|byte>: opens (creating or
+        // resuming) and, for every configuration not yet solved, logs the
+        // ranks r with (r + i) % 3 == 0 and marks it solved; prints what it did
+        // and the file's state.
+        const uint64_t configs = std::strtoull(argv[3], nullptr, 0);
+        const uint64_t names = std::strtoull(argv[4], nullptr, 0);
+        const auto kind = std::string(argv[5]) == "byte" ? d4e_host::LedgerKind::Byte
+                                                         : d4e_host::LedgerKind::Bit;
+        try {
+            d4e_host::LedgerFile f(argv[2], configs, names, kind);
+            uint64_t skipped = 0;
+            for (uint64_t i = 0; i < configs; i++) {
+                auto &c = f.config(i);
+                if (c.solved) {
+                    skipped++;
+                    continue;
+                }
+                c.shape = 0x1000 + i;
+                uint64_t n = 0;
+                for (uint64_t r = 0; r < names; r++)
+                    if ((r + i) % 3 == 0)
+                        n += f.log(r, i) ? 1u : 0u;
+                // a second log of the same pair is not new
+                if (names && f.log((3 - i % 3) % 3 < names ? (3 - i % 3) % 3 : 0, i))
+                    n += 1000;
+                c.count = n;
+                c.solved = 1 + i;
+                if (i == 1 && argc > 6 && std::string(argv[6]) == "stop")
+                    break;
+            }
+            f.sync();
+            std::printf("skipped %llu bytes %llu\n", (unsigned long long)skipped,
+                        (unsigned long long)f.bytes());
+            for (uint64_t r = 0; r < names; r++)
+                std::printf("tiled %llu %llu\n", (unsigned long long)r,
+                            (unsigned long long)f.tiled(r));
+        } catch (const std::exception &e) {
+            std::printf("error %s\n", e.what());
+            return 3;
+        }
+        return 0;
+    }
+    std::fprintf(stderr, "usage: board <file> | naming <min_m> <max_m> <min_n> <max_n> <tgt> <sizes...>"
+                         " | ledgerfile <path> <configs> <names> <bit|byte> [stop]\n");
     return 2;
 }

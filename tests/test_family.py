@@ -201,9 +201,12 @@ def test_cpp_board_matches_python(host_check, tmp_path, text):
     lines = run_check(host_check, "board", f)
     fam = F.BoardFamily.from_text(text)
     assert lines[0] == f"base {fam.base:x}"
-    assert lines[1:1 + len(fam.regions)] == [f"region {r:x}" for r in fam.regions]
-    assert lines[1 + len(fam.regions)] == f"count {fam.count} left {fam.left}"
-    assert lines[2 + len(fam.regions):] == [f"config {m:x}" for m in fam.configs()]
+    # the C++ facade keeps the reference's region order (its container's),
+    # Python the order of first appearance: same regions, same boards
+    n = len(fam.regions)
+    assert sorted(lines[1:1 + n]) == sorted(f"region {r:x}" for r in fam.regions)
+    assert lines[1 + n] == f"count {fam.count} left {fam.left}"
+    assert sorted(lines[2 + n:]) == sorted(f"config {m:x}" for m in fam.configs())
 
 
 @pytest.mark.parametrize("args", [(2, 5, 2, 8, 20, 3, 0, 7, 6), (1, 2, 0, 9, 3, 3, 2),
@@ -218,3 +221,112 @@ def test_cpp_naming_matches_python(host_check, args):
     for r, line in enumerate(lines[1:-1]):
         want = " ".join(f"{min_m + d}:{i}" for d, c in enumerate(nm.resolve(r)) for i in c)
         assert line == f"rank {r}: {want}".rstrip(), r
+
+
+@pytest.mark.parametrize("kind", ["bit", "byte"])
+def test_ledger_file_layout_and_resume(host_check, tmp_path, kind):
+    """The C++ LedgerFile writes the reference's FileBit / FileByte layout;
+    a second run skips the configurations the first one solved."""
+    import subprocess
+
+    import numpy as np
+
+    path = tmp_path / "ledger.bin"
+    configs, names = 11, 5
+    first = run_check(host_check, "ledgerfile", path, configs, names, kind, "stop")
+    assert first[0].startswith("skipped 0 ")
+    desc, tiled, logged = F.read_ledger_file(path, configs, names, kind)
+    assert list(desc[:, 2]) == [1, 2] + [0] * (configs - 2)
+    second = run_check(host_check, "ledgerfile", path, configs, names, kind)
+    assert second[0].startswith("skipped 2 ")
+    desc, tiled, logged = F.read_ledger_file(path, configs, names, kind)
+    want = np.array([[(r + i) % 3 == 0 for i in range(configs)] for r in range(names)])
+    assert (logged == want).all()
+    assert list(tiled) == list(want.sum(axis=1))
+    assert list(desc[:, 0]) == [0x1000 + i for i in range(configs)]
+    assert list(desc[:, 1]) == list(want.sum(axis=0))
+    assert list(desc[:, 2]) == [1 + i for i in range(configs)]
+    assert [ln.split()[-1] for ln in second[1:]] == [str(v) for v in tiled]
+    # a file sized for another family is refused
+    r = subprocess.run([str(host_check), "ledgerfile", str(path), str(configs + 1), str(names),
+                        kind], capture_output=True, text=True)
+    assert r.returncode == 3 and "too short" in r.stdout
+
+
+
+@pytest.fixture(scope="module")
+def family_sim(tmp_path_factory, oracle, catalogue_golden):
+    """The C++ facade with its engine calls answered by the oracle (CPU)."""
+    import shutil
+    import subprocess
+
+    from conftest import REPO
+
+    d = tmp_path_factory.mktemp("sim")
+    exe = d / "family_file_sim"
+    lib = REPO / "oracle" / "_build"
+    r = subprocess.run([shutil.which("g++") or "g++", "-O1", "-std=c++17", "-Wall", "-Werror",
+                        "-I", str(REPO / "d4-pieces_gb300" / "host"),
+                        str(REPO / "tests" / "family_file_sim.cpp"), "-o", str(exe),
+                        "-L", str(lib), "-ld4oracle", f"-Wl,-rpath,{lib}"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    pieces = d / "pieces.txt"
+    pieces.write_text("".join(f"{m} {v}\n" for m in sorted(catalogue_golden["free"])
+                              for v in catalogue_golden["free"][m]))
+    return exe, pieces
+
+
+def ledger_line(ledger):
+    return (f"ledger {len([v for v in ledger.values() if v])} {sum(ledger.values())} "
+            f"{sum((r + 1) * v for r, v in ledger.items())}")
+
+
+def test_cpp_family_file_run_matches_python(monkeypatch, oracle, family_sim, tmp_path):
+    """ac ledger, a FileBit run cut after 3 batches and resumed, and a
+    FileByte run: all equal the Python driver's ledger; each configuration's
+    logged ranks are its board's ranked combinations."""
+    import numpy as np
+
+    from d4gb import engine as E
+
+    monkeypatch.setattr(E, "batch_sets", fake_batch_sets(oracle))
+    exe, pieces = family_sim
+    text = "\naaab....\naaab....\nccdd....\nccdd....\n\n"
+    board = tmp_path / "family.txt"
+    board.write_text(text)
+    fam = F.BoardFamily.from_text(text)
+    run = F.family_ledger(fam, 2, 4, 0, 64)
+    base = [pieces, board, 2, 4, 0, 64]
+    ac = run_check(exe, *base, "ac")
+    assert ac[-1] == ledger_line(run.ledger)
+    zero = sorted(int(x.split()[-1], 16) for x in ac if x.startswith("ZERO"))
+    assert zero == sorted(run.unsolved(fam))
+    sizes = [run.naming.sizes[m] for m in range(2, 5)]
+
+    def board_ranks(m):
+        out = set()
+        for copies, _ in run.per_config[m]:
+            chosen, at = [], 0
+            for n in sizes:
+                chosen.append([j for j in range(n) if copies[at + j]])
+                at += n
+            out.add(run.naming.name(chosen))
+        return out
+
+    for kind, flag in (("bit", "fb"), ("byte", "fB")):
+        path = tmp_path / f"ledger.{kind}"
+        part = run_check(exe, *base, flag, path, 7, 3)
+        assert part[0] == "previously 0 now 21 batches 3"
+        rest = run_check(exe, *base, flag, path, 7)
+        assert rest[0] == f"previously 21 now {fam.count - 21} batches {-(-(fam.count - 21) // 7)}"
+        assert rest[-1] == ac[-1]
+        desc, tiled, logged = F.read_ledger_file(path, fam.count, run.naming.size(), kind)
+        assert tiled.tolist() == [run.ledger.get(r, 0) for r in range(run.naming.size())]
+        assert sorted(desc[:, 0].tolist()) == sorted(fam.configs())
+        for i, m in enumerate(desc[:, 0].tolist()):
+            ranks = board_ranks(m)
+            assert set(np.nonzero(logged[:, i])[0].tolist()) == ranks
+            assert desc[i, 1] == len(ranks) and desc[i, 2] > 0
+        done = run_check(exe, *base, flag, path, 7)
+        assert done[0] == f"previously {fam.count} now 0 batches 0"

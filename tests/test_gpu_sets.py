@@ -147,6 +147,7 @@ def test_family_ledger_ranks(E, oracle, rotations_only):
 def test_cpp_family_driver_matches_python(E, tmp_path):
     """The C++ facade's AtomicCount run (example_family) and the Python
     driver give the same ledger and the same ZERO-count boards."""
+    import os
     import subprocess
 
     from d4gb import build
@@ -155,8 +156,9 @@ def test_cpp_family_driver_matches_python(E, tmp_path):
     text = FAMILY + "\n"
     f = tmp_path / "family.txt"
     f.write_text(text)
+    env = {k: v for k, v in os.environ.items() if k not in ("S", "C")}
     r = subprocess.run([str(build.FAMILY_EXAMPLE_PATH), str(f), "2", "4", "0", "64"],
-                       capture_output=True, text=True, timeout=300)
+                       capture_output=True, text=True, timeout=300, env=env)
     assert r.returncode == 0, r.stderr
     lines = r.stdout.splitlines()
     fam = F.BoardFamily.from_text(text)
@@ -165,6 +167,55 @@ def test_cpp_family_driver_matches_python(E, tmp_path):
     assert ranked == len(run.ledger)
     assert total == sum(run.ledger.values())
     assert weighted == sum((k + 1) * v for k, v in run.ledger.items())
+    # the C++ facade visits configurations in the reference's region order
     zero = [int(x.split()[-1], 16) for x in lines if x.startswith("ZERO-count board")]
-    assert zero == run.unsolved(fam)
+    assert sorted(zero) == sorted(run.unsolved(fam))
     assert f"number of pieces combinations: {run.naming.size()}" in lines
+
+
+@pytest.mark.parametrize("kind", ["fb", "fB"])
+def test_cpp_family_ledger_file(E, tmp_path, kind):
+    """The FileBit / FileByte run of the C++ facade: the file holds, for
+    every configuration, exactly the ranks the Python driver finds for that
+    board, and a second run resumes with nothing left to do."""
+    import os
+    import subprocess
+
+    import numpy as np
+
+    from d4gb import build
+    from d4gb import family as F
+
+    text = FAMILY + "\n"
+    f = tmp_path / "family.txt"
+    f.write_text(text)
+    path = tmp_path / "ledger.bin"
+    env = {k: v for k, v in os.environ.items() if k != "C"}
+    env["S"] = kind
+    args = [str(build.FAMILY_EXAMPLE_PATH), str(f), "2", "4", "0", "64", str(path)]
+    first = subprocess.run(args, capture_output=True, text=True, timeout=300, env=env)
+    assert first.returncode == 0, first.stderr
+    fam = F.BoardFamily.from_text(text)
+    run = F.family_ledger(fam, 2, 4, 0, 64)
+    desc, tiled, logged = F.read_ledger_file(path, fam.count, run.naming.size(),
+                                             "byte" if kind == "fB" else "bit")
+    assert sorted(desc[:, 0].tolist()) == sorted(fam.configs())
+    assert (desc[:, 2] > 0).all()
+    assert tiled.tolist() == [run.ledger.get(r, 0) for r in range(run.naming.size())]
+    sizes = [run.naming.sizes[m] for m in range(2, 5)]
+    per_board = run.per_config
+    for i, m in enumerate(desc[:, 0].tolist()):
+        ranks = set()
+        for copies, _ in per_board[m]:
+            chosen, at = [], 0
+            for n in sizes:
+                chosen.append([j for j in range(n) if copies[at + j]])
+                at += n
+            ranks.add(run.naming.name(chosen))
+        assert set(np.nonzero(logged[:, i])[0].tolist()) == ranks, hex(m)
+        assert desc[i, 1] == len(ranks)
+    again = subprocess.run(args, capture_output=True, text=True, timeout=300, env=env)
+    assert again.returncode == 0, again.stderr
+    assert f"{fam.count}/{fam.count} configs were previously solved; solved now 0 in 0 batches" \
+        in again.stdout
+    assert again.stdout.splitlines()[-1] == first.stdout.splitlines()[-1]
