@@ -219,3 +219,18 @@ def test_cpp_family_ledger_file(E, tmp_path, kind):
     assert f"{fam.count}/{fam.count} configs were previously solved; solved now 0 in 0 batches" \
         in again.stdout
     assert again.stdout.splitlines()[-1] == first.stdout.splitlines()[-1]
+
+
+def test_sets_match_reference_fixture(E):
+    """The engine's piece sets equal the reference solver's, board by board
+    (tests/golden/sets.json: a board family's configurations and the golden
+    cases with more pieces than cells)."""
+    from d4gb.problem import Problem
+
+    data = json.loads((GOLDEN / "sets.json").read_text())
+    probs = [Problem(b["width"], b["height"], b["rows"], b["shapes"], b["counts"], b["sym"])
+             for b in data["boards"]]
+    sets, res, _ = E.batch_sets(probs)
+    for b, s, r in zip(data["boards"], sets, res):
+        assert r["status"] == 0, b["name"]
+        assert [[list(c), t] for c, t in s] == b["sets"], b["name"]

@@ -82,3 +82,29 @@ def test_check_tiling_rejects_bad_covers(oracle):
     swapped[0], swapped[1] = swapped[1], swapped[0]
     if swapped != types:
         assert not oracle.check_tiling(p, swapped, masks)              # wrong shapes
+
+
+def test_oracle_piece_sets_match_reference_fixture(oracle):
+    """Every multiset within the counts of the fixture's boards: the oracle's
+    count equals the reference solver's (tests/golden/sets.json, generated by
+    tests/golden/make_sets_golden.py from the reference's solve_count)."""
+    import itertools
+    import json
+
+    from conftest import GOLDEN
+    from d4gb.problem import Problem
+
+    data = json.loads((GOLDEN / "sets.json").read_text())
+    assert len(data["boards"]) >= 200
+    for b in data["boards"]:
+        p = Problem(b["width"], b["height"], b["rows"], b["shapes"], b["counts"], b["sym"])
+        areas = [bin(v).count("1") for v in p.shapes]
+        got = []
+        for copies in itertools.product(*[range(k + 1) for k in p.counts]):
+            if sum(a * k for a, k in zip(areas, copies)) != p.cells:
+                continue
+            n = oracle.solve_count(Problem(p.width, p.height, p.rows, p.shapes, list(copies),
+                                           p.sym))
+            if n:
+                got.append([list(copies), n])
+        assert sorted(got) == b["sets"], b["name"]
