@@ -5,8 +5,10 @@
 // configuration, the ranked combinations that tile it -- many
 // configurations per d4e_batch_sets batch.
 //
-//   [S=ac|fb|fB] [C=1] example_family <board file> <min_m> <max_m> <min_n> <max_n> [ledger file]
+//   [S=v|ac|fb|fB] [C=1] example_family <board file> <min_m> <max_m> <min_n> <max_n> [ledger file]
 //
+// S=v: the Verify searcher (the number of (configuration, combination) pairs
+// found, no ledger).
 // S=ac (default): the AtomicCount ledger in memory (configurations per rank).
 // S=fb / S=fB: the FileBit / FileByte ledger file, resumed if it exists.
 // C=1: one-sided pieces and rotations only (the reference's env C).
@@ -33,7 +35,7 @@ static void print_ledger(uint64_t names, const std::function<uint64_t(uint64_t)>
 int main(int argc, char **argv) {
     if (argc < 6) {
         std::fprintf(stderr,
-                     "usage: [S=ac|fb|fB] [C=1] %s <board file> <min_m> <max_m> <min_n> <max_n>"
+                     "usage: [S=v|ac|fb|fB] [C=1] %s <board file> <min_m> <max_m> <min_n> <max_n>"
                      " [ledger file]\n",
                      argv[0]);
         return 2;
@@ -42,11 +44,11 @@ int main(int argc, char **argv) {
     const std::string mode = env_s && *env_s ? env_s : "ac";
     const char *env_c = std::getenv("C");
     const bool one_sided = env_c && *env_c;
-    if (mode != "ac" && mode != "fb" && mode != "fB") {
-        std::fprintf(stderr, "set env S to ac|fb|fB\n");
+    if (mode != "v" && mode != "ac" && mode != "fb" && mode != "fB") {
+        std::fprintf(stderr, "set env S to v|ac|fb|fB\n");
         return 2;
     }
-    if (mode != "ac" && argc < 7) {
+    if ((mode == "fb" || mode == "fB") && argc < 7) {
         std::fprintf(stderr, "S=%s needs a ledger file\n", mode.c_str());
         return 2;
     }
@@ -61,7 +63,17 @@ int main(int argc, char **argv) {
         const d4e_host::Naming naming(min_m, max_m, min_n, max_n, board.left(), sizes);
         std::printf("number of pieces combinations: %llu\n", (unsigned long long)naming.size());
         const auto t1 = std::chrono::steady_clock::now();
-        if (mode == "ac") {
+        if (mode == "v") {
+            const auto run = d4e_host::family_ledger(board, naming, pieces, one_sided);
+            uint64_t work = 0;
+            for (uint64_t v : run.ledger)
+                work += v;
+            const auto t2 = std::chrono::steady_clock::now();
+            std::printf("%llu/%llu configurations tiled, %llu work done in %.3f ms\n",
+                        (unsigned long long)(run.configs - run.unsolved.size()),
+                        (unsigned long long)run.configs, (unsigned long long)work,
+                        std::chrono::duration<double, std::milli>(t2 - t1).count());
+        } else if (mode == "ac") {
             const auto run = d4e_host::family_ledger(board, naming, pieces, one_sided);
             std::printf("configurations %llu, distinct boards %llu, sets %llu, tilings %llu\n",
                         (unsigned long long)run.configs, (unsigned long long)run.boards,
