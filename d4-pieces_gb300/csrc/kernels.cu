@@ -5,7 +5,8 @@
 //               + impl<H> (src/kernel.cuh:12-227).  Each state is expanded by
 //               every whole-row fill -- a depth-first walk over placements
 //               anchored at the lowest empty cell of the current row, with
-//               the instance's placement table staged in shared memory -- and
+//               the instance's placement table and candidate filters read
+//               through L1 -- and
 //               each child is inserted straight into an HBM-resident
 //               open-addressing table (key CAS + 64-bit count add), which
 //               replaces the reference's ring buffer + host hash-set Sorter

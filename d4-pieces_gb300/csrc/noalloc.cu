@@ -53,9 +53,14 @@ unsigned char *scratch_address(int dev) {
 
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
-// Largest candidate-filter block of one instance: (2^W - 1 + W * 2^W)
-// bitsets of up to 4 words for W = 8.
-constexpr size_t kMaxFilterWords = (255 + 8 * 256) * 4;
+// Largest candidate-filter block of one instance (the fixed layout of
+// build_piece_lib): W * 2^(W-1) row-0 bitsets plus 2 * W * 2^W row-1 and
+// row-2 bitsets, each of ceil(placements per column / 64) words; for W = 8
+// and 255 placements per column that is (1024 + 4096) * 4 = 20480 words.
+constexpr size_t kMaxFilterWords =
+    ((size_t)kMaxWidth << (kMaxWidth - 1)) * ((kMaxPlcPerCol + 63) / 64) +
+    2 * ((size_t)kMaxWidth << kMaxWidth) * ((kMaxPlcPerCol + 63) / 64);
+static_assert(kMaxFilterWords == 20480, "filter region of the widest instance");
 
 struct Layout {
     size_t desc, seg, misc, plc, filt, front[2], cnts[2], table;
@@ -112,6 +117,13 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
             return abi_fail(e.find("more than") != std::string::npos ? D4E_ERR_UNSUPPORTED
                                                                      : D4E_ERR_INVALID,
                             e);
+        // The header regions are sized for the largest tables the builder
+        // accepts; check anyway, so that a table never spills into the
+        // frontier buffers that follow it.
+        if (lib.filters.size() > kMaxFilterWords || lib.plc.size() > (size_t)kMaxPlc)
+            return abi_fail(D4E_ERR_UNSUPPORTED,
+                            "placement or filter tables larger than the no-alloc scratch "
+                            "reserves for them");
         cudaStream_t s = static_cast<cudaStream_t>(stream);
         int dev = 0;
         cuda_check(cudaGetDevice(&dev), "cudaGetDevice");

@@ -388,8 +388,11 @@ void d4e_server_destroy(d4e_server *s);
  *
  * Works on the current CUDA device; stream may be NULL (legacy default
  * stream).  The first call on each device resolves the array's device
- * address (cudaGetSymbolAddress); make that first call before any stream
- * capture.  All calls share the array and it keeps the last call's
+ * address (cudaGetSymbolAddress) and keeps it for the life of the process,
+ * so do not call it again on a device after cudaDeviceReset.  Every call
+ * synchronises its stream after each board row (it reads the row's state
+ * count back to the host), so it must never be called while that stream is
+ * being captured.  All calls share the array and it keeps the last call's
  * contents (each call clears what it needs): calls that overlap on the GPU
  * -- from several host threads or on several streams of one device -- race
  * and must be serialised by the caller.  A puzzle whose row frontier exceeds

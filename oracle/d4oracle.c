@@ -529,6 +529,41 @@ static double now_s(void)
     return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
 }
 
+/* Placements anchored at (row 0, col) of the W-stride board, anchor = the
+ * placement's lowest cell (the order of Piece::cover's anchors,
+ * src/Piece.inl:5-24); each carries its type's copy bits. */
+static void dp_build_tab(const or_ctx *cp, dp_tab *tp)
+{
+    const or_ctx c = *cp;
+    memset(tp, 0, sizeof(*tp));
+    tp->W = c.W;
+    tp->H = c.H;
+    tp->board = c.board;
+    int base = 0;
+    for (int i = 0; i < c.n; i++) {
+        const or_piece *pc = &c.lib[i];
+        uint64_t tm = pc->count ? (((pc->count >= 64) ? ~0ull : ((1ull << pc->count) - 1)) << base) : 0;
+        base += (int)pc->count;
+        for (int t = 0; t < pc->nplc; t++) {
+            const or_plc *pl = &pc->plc[t];
+            if (!pl->enabled || !tm)
+                continue;
+            for (int col = 0; col < c.W; col++) {
+                int x = col - pl->cc[0];
+                if (x < 0 || x + pl->w > c.W || pl->h > c.H)
+                    continue;
+                u128 m = plc_mask(&c, pl, 0, x);
+                tp->plc[col] = (dp_plc *)realloc(tp->plc[col], (size_t)(tp->nplc[col] + 1) * sizeof(dp_plc));
+                dp_plc *d = &tp->plc[col][tp->nplc[col]++];
+                d->rel = (uint64_t)m;
+                d->rel_hi = (uint64_t)(m >> 64);
+                d->tmask = tm;
+                d->h = pl->h;
+            }
+        }
+    }
+}
+
 int32_t or_rowdp(const or_problem *p, int32_t threads, double max_seconds,
                  uint64_t max_children, uint64_t *level_sizes, uint64_t *count,
                  int32_t *levels_done, uint64_t *states_total)
@@ -546,34 +581,7 @@ int32_t or_rowdp(const or_problem *p, int32_t threads, double max_seconds,
         return -1;
     }
     dp_tab tab;
-    memset(&tab, 0, sizeof(tab));
-    tab.W = c.W;
-    tab.H = c.H;
-    tab.board = c.board;
-    /* Placements anchored at (row 0, col): anchor = lowest cell. */
-    int base = 0;
-    for (int i = 0; i < c.n; i++) {
-        const or_piece *pc = &c.lib[i];
-        uint64_t tm = pc->count ? (((pc->count >= 64) ? ~0ull : ((1ull << pc->count) - 1)) << base) : 0;
-        base += (int)pc->count;
-        for (int t = 0; t < pc->nplc; t++) {
-            const or_plc *pl = &pc->plc[t];
-            if (!pl->enabled || !tm)
-                continue;
-            for (int col = 0; col < c.W; col++) {
-                int x = col - pl->cc[0];
-                if (x < 0 || x + pl->w > c.W || pl->h > c.H)
-                    continue;
-                u128 m = plc_mask(&c, pl, 0, x);
-                tab.plc[col] = (dp_plc *)realloc(tab.plc[col], (size_t)(tab.nplc[col] + 1) * sizeof(dp_plc));
-                dp_plc *d = &tab.plc[col][tab.nplc[col]++];
-                d->rel = (uint64_t)m;
-                d->rel_hi = (uint64_t)(m >> 64);
-                d->tmask = tm;
-                d->h = pl->h;
-            }
-        }
-    }
+    dp_build_tab(&c, &tab);
     int T = threads;
     dp_vec cur = { 0, 0, 0 };
     dp_state root = { c.board, 0, 1 };
@@ -700,6 +708,262 @@ int32_t or_rowdp(const or_problem *p, int32_t threads, double max_seconds,
         free(tab.plc[col]);
     free(c.lib);
     return 0;
+}
+
+/* ------------------------------------------------------------------------
+ * Memory-lean exact row DP: the same levels, whole-row fills and
+ * de-duplication as or_rowdp (src/searcher_cuda.cu:32-82,
+ * src/kernel.cuh:12-49), but children go straight into hash shards (one lock
+ * each, filled through small per-thread buffers) instead of being stored
+ * before a merge, so memory holds the distinct states only.
+ * ---------------------------------------------------------------------- */
+#define LEAN_SHARD_BITS 12
+#define LEAN_SHARDS (1u << LEAN_SHARD_BITS)
+#define LEAN_BUF 16
+
+typedef struct {
+    pthread_mutex_t mu;
+    dp_state *tab; /* cnt == 0: empty slot (every state reaches here with cnt >= 1) */
+    size_t cap, n;
+} lean_shard;
+
+typedef struct {
+    const dp_tab *tab;
+    int row;
+    const dp_state *in;
+    size_t n_in;
+    size_t *next;       /* shared work cursor (chunks of parents) */
+    lean_shard *shards;
+    dp_state *buf;      /* LEAN_SHARDS x LEAN_BUF */
+    uint8_t *bufn;
+    uint64_t cnt;       /* multiplicity of the parent being expanded */
+    uint64_t raw;       /* children produced */
+} lean_worker;
+
+static void lean_shard_put(lean_shard *sh, const dp_state *s, uint64_t h)
+{
+    size_t i = (size_t)h & (sh->cap - 1);
+    for (;;) {
+        dp_state *t = &sh->tab[i];
+        if (!t->cnt) {
+            *t = *s;
+            sh->n++;
+            return;
+        }
+        if (t->open == s->open && t->used == s->used) {
+            t->cnt += s->cnt;
+            return;
+        }
+        i = (i + 1) & (sh->cap - 1);
+    }
+}
+
+static void lean_shard_grow(lean_shard *sh)
+{
+    size_t oc = sh->cap;
+    dp_state *old = sh->tab;
+    sh->cap = oc ? oc * 2 : 1024;
+    sh->tab = (dp_state *)calloc(sh->cap, sizeof(dp_state));
+    sh->n = 0;
+    for (size_t i = 0; i < oc; i++)
+        if (old[i].cnt)
+            lean_shard_put(sh, &old[i], dp_hash(&old[i]));
+    free(old);
+}
+
+static void lean_flush(lean_worker *w, uint32_t b)
+{
+    lean_shard *sh = &w->shards[b];
+    pthread_mutex_lock(&sh->mu);
+    if ((sh->n + w->bufn[b]) * 10 > sh->cap * 6)
+        lean_shard_grow(sh);
+    for (uint32_t k = 0; k < w->bufn[b]; k++) {
+        const dp_state *s = &w->buf[(size_t)b * LEAN_BUF + k];
+        lean_shard_put(sh, s, dp_hash(s));
+    }
+    pthread_mutex_unlock(&sh->mu);
+    w->bufn[b] = 0;
+}
+
+/* dp_fill with the child sent to its shard's buffer. */
+static void lean_fill(lean_worker *w, u128 open, uint64_t used)
+{
+    const dp_tab *t = w->tab;
+    int W = t->W;
+    u128 rowm = (((u128)1 << W) - 1) << (w->row * W);
+    if (!(open & rowm)) {
+        dp_state s = { open, used, w->cnt };
+        uint32_t b = (uint32_t)(dp_hash(&s) >> (64 - LEAN_SHARD_BITS));
+        w->buf[(size_t)b * LEAN_BUF + w->bufn[b]++] = s;
+        if (w->bufn[b] == LEAN_BUF)
+            lean_flush(w, b);
+        w->raw++;
+        return;
+    }
+    int pos = ctz128(open);
+    int col = pos % W;
+    for (int i = 0; i < t->nplc[col]; i++) {
+        const dp_plc *pl = &t->plc[col][i];
+        if (w->row + pl->h > t->H)
+            continue;
+        u128 m = (((u128)pl->rel_hi << 64) | pl->rel) << (w->row * W);
+        if (m & ~open)
+            continue;
+        uint64_t tm = pl->tmask;
+        uint64_t nb = ((used & tm) + (tm & (~tm + 1))) & tm;
+        if (!nb)
+            continue;
+        lean_fill(w, open & ~m, used | nb);
+    }
+}
+
+static void *lean_worker_run(void *arg)
+{
+    lean_worker *w = (lean_worker *)arg;
+    const size_t chunk = 4096;
+    for (;;) {
+        size_t lo = __atomic_fetch_add(w->next, chunk, __ATOMIC_RELAXED);
+        if (lo >= w->n_in)
+            break;
+        size_t hi = lo + chunk < w->n_in ? lo + chunk : w->n_in;
+        for (size_t i = lo; i < hi; i++) {
+            w->cnt = w->in[i].cnt;
+            lean_fill(w, w->in[i].open, w->in[i].used);
+        }
+    }
+    for (uint32_t b = 0; b < LEAN_SHARDS; b++)
+        if (w->bufn[b])
+            lean_flush(w, b);
+    return NULL;
+}
+
+typedef struct {
+    lean_shard *shards;
+    uint32_t lo, hi;
+    const size_t *offs;
+    dp_state *out;
+} lean_collect_job;
+
+static void *lean_collect_run(void *arg)
+{
+    lean_collect_job *j = (lean_collect_job *)arg;
+    for (uint32_t b = j->lo; b < j->hi; b++) {
+        lean_shard *sh = &j->shards[b];
+        dp_state *o = j->out + j->offs[b];
+        for (size_t i = 0; i < sh->cap; i++)
+            if (sh->tab[i].cnt)
+                *o++ = sh->tab[i];
+        free(sh->tab);
+        sh->tab = NULL;
+        sh->cap = sh->n = 0;
+    }
+    return NULL;
+}
+
+int32_t or_rowdp_lean(const or_problem *p, int32_t threads, uint64_t *level_sizes,
+                      uint64_t *raw_sizes, uint64_t *count, double *seconds)
+{
+    or_ctx c;
+    if (build_ctx(p, &c))
+        return -1;
+    if (threads < 1)
+        threads = 1;
+    int copies = 0;
+    for (int i = 0; i < c.n; i++)
+        copies += (int)c.lib[i].count;
+    if (copies > OR_MAX_COPIES) {
+        free(c.lib);
+        return -1;
+    }
+    dp_tab tab;
+    dp_build_tab(&c, &tab);
+    const double t0 = now_s();
+    const int T = threads;
+    lean_shard *shards = (lean_shard *)calloc(LEAN_SHARDS, sizeof(lean_shard));
+    for (uint32_t b = 0; b < LEAN_SHARDS; b++)
+        pthread_mutex_init(&shards[b].mu, NULL);
+    lean_worker *ws = (lean_worker *)calloc((size_t)T, sizeof(lean_worker));
+    for (int k = 0; k < T; k++) {
+        ws[k].buf = (dp_state *)malloc((size_t)LEAN_SHARDS * LEAN_BUF * sizeof(dp_state));
+        ws[k].bufn = (uint8_t *)calloc(LEAN_SHARDS, 1);
+    }
+    pthread_t *th = (pthread_t *)calloc((size_t)T, sizeof(pthread_t));
+    size_t n_cur = 1;
+    dp_state *cur = (dp_state *)malloc(sizeof(dp_state));
+    cur[0].open = c.board;
+    cur[0].used = 0;
+    cur[0].cnt = 1;
+    int32_t rc = 0;
+    for (int r = 0; r < c.H; r++) {
+        size_t next = 0;
+        for (int k = 0; k < T; k++) {
+            ws[k].tab = &tab;
+            ws[k].row = r;
+            ws[k].in = cur;
+            ws[k].n_in = n_cur;
+            ws[k].next = &next;
+            ws[k].shards = shards;
+            ws[k].raw = 0;
+            pthread_create(&th[k], NULL, lean_worker_run, &ws[k]);
+        }
+        uint64_t raw = 0;
+        for (int k = 0; k < T; k++) {
+            pthread_join(th[k], NULL);
+            raw += ws[k].raw;
+        }
+        free(cur);
+        size_t *offs = (size_t *)calloc(LEAN_SHARDS + 1, sizeof(size_t));
+        for (uint32_t b = 0; b < LEAN_SHARDS; b++)
+            offs[b + 1] = offs[b] + shards[b].n;
+        n_cur = offs[LEAN_SHARDS];
+        cur = (dp_state *)malloc((n_cur ? n_cur : 1) * sizeof(dp_state));
+        if (!cur) {
+            rc = -2;
+            free(offs);
+            break;
+        }
+        lean_collect_job *jobs = (lean_collect_job *)calloc((size_t)T, sizeof(lean_collect_job));
+        for (int k = 0; k < T; k++) {
+            jobs[k].shards = shards;
+            jobs[k].lo = (uint32_t)((uint64_t)LEAN_SHARDS * (uint64_t)k / (uint64_t)T);
+            jobs[k].hi = (uint32_t)((uint64_t)LEAN_SHARDS * (uint64_t)(k + 1) / (uint64_t)T);
+            jobs[k].offs = offs;
+            jobs[k].out = cur;
+            pthread_create(&th[k], NULL, lean_collect_run, &jobs[k]);
+        }
+        for (int k = 0; k < T; k++)
+            pthread_join(th[k], NULL);
+        free(jobs);
+        free(offs);
+        if (level_sizes)
+            level_sizes[r] = n_cur;
+        if (raw_sizes)
+            raw_sizes[r] = raw;
+    }
+    uint64_t cnt = 0;
+    if (rc == 0)
+        for (size_t i = 0; i < n_cur; i++)
+            cnt += cur[i].cnt;
+    if (count)
+        *count = cnt;
+    if (seconds)
+        *seconds = now_s() - t0;
+    free(cur);
+    for (int k = 0; k < T; k++) {
+        free(ws[k].buf);
+        free(ws[k].bufn);
+    }
+    free(ws);
+    free(th);
+    for (uint32_t b = 0; b < LEAN_SHARDS; b++) {
+        pthread_mutex_destroy(&shards[b].mu);
+        free(shards[b].tab);
+    }
+    free(shards);
+    for (int col = 0; col < 11; col++)
+        free(tab.plc[col]);
+    free(c.lib);
+    return rc;
 }
 
 /* ------------------------------------------------------------------------

@@ -23,7 +23,9 @@
  *     every set of placements anchored in the current row that covers all
  *     of its empty cells (no L/R half split, no island pruning), states
  *     de-duplicated per level with tiling multiplicities summed.  It yields
- *     per-level frontier sizes and the tiling count.
+ *     per-level frontier sizes and the tiling count.  or_rowdp_lean is the
+ *     same DP with children de-duplicated as they are produced (for
+ *     frontiers of 10^8 states and more).
  *
  * Parity of (1) is pinned against the reference's own solver, compiled from
  * the reference sources by oracle/Makefile into oracle/_ref/d4ref, through
@@ -78,6 +80,17 @@ void or_canonical_grid(const or_problem *p, const int8_t *grid, int8_t *out);
 int32_t or_rowdp(const or_problem *p, int32_t threads, double max_seconds,
                  uint64_t max_children, uint64_t *level_sizes, uint64_t *count,
                  int32_t *levels_done, uint64_t *states_total);
+
+/* The same exact row DP with bounded memory: children are de-duplicated as
+ * they are produced (hash shards with one lock each) instead of stored
+ * first, so memory holds each level's distinct states only (32 bytes each,
+ * plus the shards' free slots).  level_sizes[r] = distinct states after
+ * row r, raw_sizes[r] = children produced while completing row r (either
+ * may be NULL); *count = tilings (mod 2^64); *seconds = elapsed time.
+ * Runs every row to the end.  Returns 0, -1 on bad input, -2 when host
+ * memory ran out. */
+int32_t or_rowdp_lean(const or_problem *p, int32_t threads, uint64_t *level_sizes,
+                      uint64_t *raw_sizes, uint64_t *count, double *seconds);
 
 /* Independent cover check of one tiling given as placements:
  * piece type + cell mask (lo/hi 64-bit halves of the W-stride bitboard).

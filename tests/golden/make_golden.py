@@ -16,6 +16,7 @@ the GPU machine: the fixtures are committed.
 from __future__ import annotations
 
 import json
+import os
 import random
 import subprocess
 import sys
@@ -109,7 +110,9 @@ def fixed_cases(cat) -> list:
 
 
 def main() -> None:
-    ref_src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src"
+    ref_src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("D4_REFERENCE_SRC", "")
+    if not ref_src:
+        sys.exit("usage: make_golden.py <reference src dir> (or set D4_REFERENCE_SRC)")
     subprocess.run(["make", "-s", "-C", str(REPO / "oracle"), "ref", f"REF={ref_src}"], check=True)
     cat_out = run_ref(Problem(1, 1, [1], [], [], FULL_D4), "catalogue")
     cat = {"free": {}, "onesided": {}}

@@ -26,6 +26,18 @@ def test_rowdp_count_matches_reference(oracle, case):
     assert r["count"] == case["count"]
 
 
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_lean_rowdp_matches_reference_and_rowdp(oracle, case):
+    """The memory-lean DP (used to pin the 8x15 enumeration) gives the
+    reference's count and the same per-row frontier sizes as the stored-
+    children DP."""
+    p = case_problem(case)
+    lean = oracle.rowdp_lean(p, threads=3)
+    full = oracle.rowdp(p, threads=2)
+    assert lean["count"] == case["count"]
+    assert lean["level_sizes"] == full["level_sizes"]
+
+
 LISTED = [c for c in CASES if "solutions" in c]
 
 

@@ -57,6 +57,38 @@ def test_noalloc_alternating_puzzles(E):
         assert E.count_noalloc(b) == want_b
 
 
+def wide_table_problems(E):
+    """8-wide puzzles whose columns hold more than 64 placements, so their
+    candidate filters take 2 or 4 words per bitset: the largest tables the
+    array has to hold (the 35 hexominoes: 214 placements at column 3)."""
+    from d4gb.problem import Problem, single_large
+
+    hexo = E.catalogue(6)
+    sl = single_large(3)
+    return [
+        Problem(8, 3, [0xFF] * 3, hexo, [1] * len(hexo), 0xFF, name="35 hexominoes 8x3"),
+        Problem(8, 4, [0xFF] * 4, sl.shapes, [1] * len(sl.shapes), 0xFF,
+                name="13 types of the 8x15 set, 8x4"),
+        Problem(8, 5, [0xFF, 0xFF, 0xE7, 0xFF, 0xFF], sl.shapes, [1] * len(sl.shapes), 0xFF,
+                name="13 types of the 8x15 set, 8x5 minus 2"),
+    ]
+
+
+@pytest.mark.parametrize("which", [0, 1, 2])
+def test_noalloc_wide_placement_tables(E, oracle, which):
+    """Multi-word candidate filters fit the array and leave the frontier
+    buffers after them intact: the count and the states equal the
+    searcher's and the oracle's, on two calls in a row."""
+    p = wide_table_problems(E)[which]
+    f = E.Frow(p.shapes, p.counts, p.sym, p.width, device=None)
+    assert max(f.placements(c) for c in range(p.width)) > 64
+    want = searcher_count(E, p)
+    ref = oracle.rowdp(p, threads=4)
+    assert want == (ref["count"], sum(ref["level_sizes"]))
+    assert E.count_noalloc(p) == want
+    assert E.count_noalloc(p) == want
+
+
 def test_noalloc_rejects_frontier_beyond_capacity(E):
     from d4gb.problem import medium_board
 
