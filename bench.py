@@ -36,8 +36,19 @@ sys.path.insert(0, str(REPO))
 # (within the required 1e8..1e9; seeds 0..4 scanned on a GB300: seed 2 peaks
 # at 514M, seed 4 above 1e9) and it has 437,783,699,473,187 tilings.
 SINGLE_LARGE_SEED = 3
-CPU_SAMPLE_MAX_CHILDREN = 150_000_000  # bounds the CPU sample's host memory (~10 GB)
 L2_FLUSH_BYTES = 512 << 20
+# Rows the CPU baselines time on the single large puzzle: rows 0..3 in full
+# (42.5M distinct states; some seconds on a 16-core host).  The GPU's states/s
+# over the same rows is reported beside them, so the two compare like for like.
+SAME_ROWS = 4
+ALG_RECORD_BYTES = 24   # per-state record of the roofline's algorithmic bytes
+# Batched mix and serving sections of the default run (the other configs of
+# the headline metric: batched vs plain puzzles/s, served vs plain p50/p99).
+MIX_INSTANCES = 8192
+MIX_MAX_STATES = 0            # no per-instance row limit: every instance counted
+SERVE_SECONDS = 2.0           # 2000 req/s arrival window (4000 requests)
+SERVE_LIGHT_SECONDS = 10.0    # 60 req/s arrival window (600 requests)
+SERVE_GRACE = 15.0            # seconds after the window before unfinished requests are cut
 
 
 def parse_args():
@@ -67,6 +78,16 @@ def parse_args():
     ap.add_argument("--cpu-budget", type=float, default=15.0,
                     help="seconds of host CPU work for the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mix-instances", type=int, default=MIX_INSTANCES,
+                    help="default run: instances of the batched mix (counting and solve-one)")
+    ap.add_argument("--mix-max-states", type=int, default=MIX_MAX_STATES,
+                    help="default run: per-instance row limit in the batched mix sections")
+    ap.add_argument("--serve-seconds", type=float, default=SERVE_SECONDS,
+                    help="default run: arrival window of the 2000 req/s serving section")
+    ap.add_argument("--serve-light-seconds", type=float, default=SERVE_LIGHT_SECONDS,
+                    help="default run: arrival window of the 60 req/s serving section")
+    ap.add_argument("--no-mix", action="store_true",
+                    help="default run: skip the batched mix and serving sections")
     ap.add_argument("--autotune", action="store_true",
                     help="measure launch plans in the first warm-up step (D4E_AUTOTUNE); "
                          "the default plan is the one the tuner keeps on this workload")
@@ -226,21 +247,105 @@ def run_once(E, prob, device: int, autotune: bool = False) -> dict:
     return {"wall_s": wall, "count": count, "stats": st, "levels": levels}
 
 
-def cpu_baseline(prob, budget: float) -> dict:
+def cpu_model() -> str:
+    try:
+        for ln in Path("/proc/cpuinfo").read_text().splitlines():
+            k, _, v = ln.partition(":")
+            if k.strip() in ("model name", "Model", "CPU part"):
+                return v.strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
+def cpu_same_rows(prob) -> dict:
+    """The oracle's exact row DP (restating the reference's level search) on
+    rows 0..SAME_ROWS-1 of the puzzle, in full, on every host core."""
     from oracle import pyoracle
 
     pyoracle.build()
     threads = os.cpu_count() or 1
+    r = pyoracle.rowdp_lean(prob, threads=threads, max_rows=SAME_ROWS)
+    states = sum(r["level_sizes"])
+    return {"value": states / r["seconds"], "unit": "states/s", "cores": threads,
+            "kind": "port", "cpu": cpu_model(), "rows": f"0-{SAME_ROWS - 1}",
+            "states": states, "seconds": r["seconds"], "level_sizes": r["level_sizes"],
+            "sample": (f"exact row DP (oracle/, restating the reference's level search "
+                       f"src/searcher_cuda.cu:32-82 with whole-row fills) on rows "
+                       f"0-{SAME_ROWS - 1} of {prob.height} of the same puzzle, in full: "
+                       f"{states} distinct states in {r['seconds']:.1f} s on {threads} threads")}
+
+
+def cpu_backtracker(E, threads: int | None = None) -> dict:
+    """The reference's own CPU algorithm -- the backtracking solve_count
+    (src/Piece.cpp:104-139), as the oracle restates it -- on the pentomino
+    ring (the 8x8 board minus its centre 2x2, 12 pentominoes, 520 tilings):
+    one puzzle per host thread, all threads at once (the solver is
+    single-threaded; the reference runs its puzzles in parallel)."""
+    from d4gb.problem import pentomino_ring
+    from oracle import pyoracle
+
+    pyoracle.build()
+    threads = threads or os.cpu_count() or 1
+    ring = pentomino_ring(E.catalogue(5))
+    counts = [None] * threads
+
+    def work(i):
+        counts[i] = pyoracle.solve_count(ring)
+
     t0 = time.perf_counter()
-    r = pyoracle.rowdp(prob, threads=threads, max_seconds=budget,
-                       max_children=CPU_SAMPLE_MAX_CHILDREN)
+    ths = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
     el = time.perf_counter() - t0
-    return {"value": r["states_total"] / el if el > 0 else None, "unit": "states/s",
-            "cores": threads, "kind": "port",
-            "sample": (f"exact row DP (oracle/, restating the reference's level search) on the "
-                       f"same puzzle: rows 1-{r['levels_done']} of {prob.height} and part of the "
-                       f"next, {r['states_total']} frontier states expanded in {el:.1f} s on "
-                       f"{threads} threads")}
+    if any(c != 520 for c in counts):
+        raise RuntimeError(f"backtracker counts {set(counts)} != 520")
+    return {"value": threads / el, "unit": "puzzles/s", "cores": threads, "kind": "port",
+            "cpu": cpu_model(), "seconds": el,
+            "sample": (f"{threads} pentomino-ring puzzles (520 tilings each) counted by the "
+                       f"backtracker restatement, one per host thread, in {el:.1f} s")}
+
+
+def gpu_same_rows(E, prob, device: int, reps: int = 3) -> dict:
+    """The engine on rows 0..SAME_ROWS-1 of the puzzle (one search_GPU per
+    row, each synchronised), fastest of `reps`."""
+    best = None
+    for _ in range(reps):
+        f = E.Frow(prob.shapes, prob.counts, prob.sym, prob.width, device=device)
+        s = E.CudaSearcher(f, rows=prob.rows)
+        t0 = time.perf_counter()
+        for _ in range(SAME_ROWS):
+            s.search_GPU()
+        el = time.perf_counter() - t0
+        states = sum(s.level_sizes()[:SAME_ROWS])
+        del s, f
+        best = el if best is None else min(best, el)
+    return {"value": states / best, "unit": "states/s", "rows": f"0-{SAME_ROWS - 1}",
+            "states": states, "seconds": best}
+
+
+def gpu_ring(E, device: int, reps: int = 5) -> dict:
+    """The plain single-puzzle path on the pentomino ring, fastest of reps."""
+    from d4gb.problem import pentomino_ring
+
+    ring = pentomino_ring(E.catalogue(5))
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        f = E.Frow(ring.shapes, ring.counts, ring.sym, ring.width, device=device)
+        s = E.CudaSearcher(f, rows=ring.rows)
+        s.run()
+        n = s.count()
+        el = time.perf_counter() - t0
+        del s, f
+        if n != 520:
+            raise RuntimeError(f"ring count {n} != 520")
+        best = el if best is None else min(best, el)
+    return {"value": 1.0 / best, "unit": "puzzles/s", "seconds": best}
 
 
 def make_problem(args):
@@ -285,7 +390,12 @@ def bench_ours(args, dist: Dist) -> None:
     st = [r["stats"] for r in runs]
     exp_ms = sum(s["expand_ms"] for s in st)
     exp_launches = sum(s["expand_launches"] for s in st)
-    alg_bytes = sum(s["record_bytes"] * (s["states_in"] + s["states_raw"]) for s in st)
+    # Algorithmic bytes of the expansion: S = 24 B per state record (window
+    # u64 + used u32 + instance u32 + count u64) x (parents read + raw
+    # children written), the per-state figure the level search is costed
+    # with; the packed records here are 16 B, so this counts 1.5x the bytes
+    # they actually occupy.
+    alg_bytes = sum(ALG_RECORD_BYTES * (s["states_in"] + s["states_raw"]) for s in st)
     peaks = measured_peaks()
     achieved = alg_bytes / (exp_ms / 1e3) / 1e9 if exp_ms > 0 else None
     traffic = profiled_traffic()
@@ -355,6 +465,7 @@ def bench_ours(args, dist: Dist) -> None:
             "frac": achieved / peaks["hbm_gbs"] if achieved else None,
             "traffic": traffic_per_launch,
             "algorithmic_bytes_per_launch": alg_bytes / exp_launches if exp_launches else None,
+            "algorithmic_bytes": "24 B x (parent states read + raw children inserted) per launch",
             "avg_launch_ms": exp_ms / exp_launches if exp_launches else None,
             "launches": exp_launches,
         },
@@ -372,7 +483,33 @@ def bench_ours(args, dist: Dist) -> None:
         "clocks": clocks,
     }
     if not args.no_cpu_baseline and dist.world == 1:
-        line["cpu_baseline"] = cpu_baseline(prob, args.cpu_budget)
+        # Like for like: the CPU restatement and the engine on the same whole
+        # rows (0..SAME_ROWS-1), and the reference's backtracker against the
+        # engine on the pentomino ring.
+        cpu = cpu_same_rows(prob)
+        gpu = gpu_same_rows(E, prob, dev)
+        line["cpu_baseline"] = cpu
+        line["same_rows"] = {"rows": cpu["rows"], "gpu_states_per_s": gpu["value"],
+                             "cpu_states_per_s": cpu["value"],
+                             "ratio": gpu["value"] / cpu["value"],
+                             "full_run_ratio": line["value"] / cpu["value"]}
+        bt = cpu_backtracker(E)
+        ring = gpu_ring(E, dev)
+        line["pentomino_ring"] = {"cpu_backtracker": bt, "gpu_plain_puzzles_per_s": ring["value"],
+                                  "gpu_seconds": ring["seconds"],
+                                  "ratio_vs_all_cores": ring["value"] / bt["value"]}
+    if not args.no_mix and dist.world == 1:
+        # The headline metric's other configurations: the batched mix
+        # (counting, then solve-one) and serving, each against the plain
+        # one-puzzle-at-a-time path.
+        line["batched_count"] = mix_section(E, dev, args.mix_instances, E.MODE_COUNT,
+                                            args.mix_max_states, MIX_BEAM)
+        line["batched_solve_one"] = mix_section(E, dev, args.mix_instances, E.MODE_SOLVE_ONE,
+                                                args.mix_max_states, MIX_BEAM)
+        line["served"] = serve_section(E, dev, 2000.0, args.serve_seconds, args.mix_max_states,
+                                       MIX_BEAM, SERVE_GRACE)
+        line["served_light"] = serve_section(E, dev, 60.0, args.serve_light_seconds,
+                                             args.mix_max_states, MIX_BEAM, SERVE_GRACE)
     print(json.dumps(line), flush=True)
 
 
@@ -387,24 +524,21 @@ def bench_reference(args, dist: Dist) -> None:
     pyoracle.build()
     prob, workload = make_problem(args)
     threads = os.cpu_count() or 1
-    per_step = max(2.0, min(args.cpu_budget, 150.0 / max(args.steps + args.warmup, 1)))
+    # A step = rows 0..SAME_ROWS-1 of the puzzle in full (the ours arm's line
+    # reports the GPU's states/s over the same rows as same_rows).
     for _ in range(args.warmup):
-        pyoracle.rowdp(prob, threads=threads, max_seconds=per_step,
-                       max_children=CPU_SAMPLE_MAX_CHILDREN)
+        pyoracle.rowdp_lean(prob, threads=threads, max_rows=SAME_ROWS)
     states = 0
     t0 = time.perf_counter()
-    done = []
     for _ in range(args.steps):
-        r = pyoracle.rowdp(prob, threads=threads, max_seconds=per_step,
-                           max_children=CPU_SAMPLE_MAX_CHILDREN)
-        states += r["states_total"]
-        done.append(r["levels_done"])
+        r = pyoracle.rowdp_lean(prob, threads=threads, max_rows=SAME_ROWS)
+        states += sum(r["level_sizes"])
     el = time.perf_counter() - t0
     v = states / el if el > 0 else None
     sample = (f"exact row DP (oracle/ restating the reference's level search, "
               f"src/searcher_cuda.cu + src/kernel.cuh, with whole-row fills) on the same "
-              f"puzzle: per step rows 1-{min(done)} of {prob.height} and part of the next, "
-              f"{per_step:.0f} s budget, {threads} threads")
+              f"puzzle: per step rows 0-{SAME_ROWS - 1} of {prob.height} in full, "
+              f"{threads} threads ({cpu_model()})")
     print(json.dumps({
         "impl": "reference",
         "metric": "frontier states/s (exact enumeration, single large 8x15 puzzle)",
@@ -419,9 +553,11 @@ def bench_reference(args, dist: Dist) -> None:
         "vs_baseline": None,
         "dtype": "u64",
         "data": "synthetic (seeded generator d4gb.problem.single_large)",
-        "config": {"workload": workload, "parallelism": f"host threads x{threads}"},
+        "config": {"workload": workload, "parallelism": f"host threads x{threads}",
+                   "rows": f"0-{SAME_ROWS - 1} of {prob.height} (the ours arm reports the "
+                           f"GPU on the same rows as same_rows)"},
         "cpu_baseline": {"value": v, "unit": "states/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+                         "cpu": cpu_model(), "sample": sample},
         "e2e": {"value": v, "unit": "states/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -691,6 +827,198 @@ def bench_serve(args, dist: Dist) -> None:
             "speedup_vs_plain": (len(done) / elapsed) / plain_rate,
             "cover_checked": sum(1 for r in done if r["found"]),
         }), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# batched mix and serving sections of the default run
+# ---------------------------------------------------------------------------
+MIX_BEAM = 1024
+
+
+def _service_times(out) -> list[float]:
+    """Per-instance service times (ms) of a sequential batch_run: its
+    latencies are cumulative from the batch start, in instance order."""
+    prev, svc = 0.0, []
+    for r in out:
+        svc.append(r["latency_ms"] - prev)
+        prev = r["latency_ms"]
+    return svc
+
+
+def mix_section(E, dev: int, n: int, mode: int, max_states: int, beam: int) -> dict:
+    """Config 3 (counting) or config 4 (solve-one): the batched mix run as one
+    batch and one puzzle at a time (the plain path: the same engine, one
+    launch sequence per puzzle), results compared instance by instance.
+    Amdahl split: the 10 % of instances with the longest plain service time,
+    and the rest, each also run as a batch of its own."""
+    from d4gb.problem import batched_mix, verify_tiling
+
+    probs = batched_mix(BATCHED_SEED, n)
+    arms, outs = {}, {}
+    for arm, seq in (("batched", False), ("plain", True)):
+        t0 = time.perf_counter()
+        out, st = E.batch_run(probs, mode=mode, sequential=seq, device=dev,
+                              max_states=max_states, beam=beam)
+        wall = time.perf_counter() - t0
+        outs[arm] = out
+        arms[arm] = {"wall_s": wall, "puzzles_per_s": n / wall,
+                     "states_per_s": st["states_out"] / wall, "states": st["states_out"],
+                     "completed": sum(1 for r in out if r["status"] == 0),
+                     "expand_launches": st["expand_launches"],
+                     "compact_launches": st["compact_launches"],
+                     "expand_ms": st["expand_ms"], "compact_ms": st["compact_ms"],
+                     "peak_frontier": st["peak_frontier"]}
+    for a, b in zip(outs["batched"], outs["plain"]):
+        if (a["status"], a["count"], a["found"]) != (b["status"], b["count"], b["found"]):
+            raise RuntimeError("batched and plain results differ")
+    failed = [i for i, r in enumerate(outs["batched"]) if r["status"] != 0]
+    sec = {"instances": n, "seed": BATCHED_SEED, "max_states_per_row": max_states,
+           "batched": arms["batched"], "plain": arms["plain"],
+           "speedup_vs_plain": arms["batched"]["puzzles_per_s"] / arms["plain"]["puzzles_per_s"],
+           "failed": len(failed),
+           "failed_status": sorted({outs["batched"][i]["status"] for i in failed})}
+    if mode == E.MODE_SOLVE_ONE:
+        found = [i for i, r in enumerate(outs["batched"]) if r["found"]]
+        bad = sum(1 for i in found
+                  if not verify_tiling(probs[i], outs["batched"][i]["grid"],
+                                       outs["batched"][i]["steps"]))
+        if bad:
+            raise RuntimeError(f"{bad} solve-one tilings fail the cover check")
+        sec["found"] = len(found)
+        sec["cover_checked"] = len(found)
+        sec["beam"] = beam
+    else:
+        sec["tilings"] = sum(r["count"] for r in outs["batched"] if r["status"] == 0)
+    # Amdahl split on the plain service times.
+    svc = _service_times(outs["plain"])
+    order = sorted(range(n), key=lambda i: -svc[i])
+    top = sorted(order[: max(1, n // 10)])
+    rest = sorted(order[max(1, n // 10):])
+    split = {"plain_ms_top10pct": sum(svc[i] for i in top),
+             "plain_ms_rest": sum(svc[i] for i in rest)}
+    for name, idx in (("top10pct", top), ("rest", rest)):
+        t0 = time.perf_counter()
+        E.batch_run([probs[i] for i in idx], mode=mode, device=dev, max_states=max_states,
+                    beam=beam)
+        split[f"batched_ms_{name}"] = (time.perf_counter() - t0) * 1e3
+    split["speedup_top10pct"] = split["plain_ms_top10pct"] / split["batched_ms_top10pct"]
+    split["speedup_rest"] = split["plain_ms_rest"] / split["batched_ms_rest"]
+    split["plain_share_top10pct"] = split["plain_ms_top10pct"] / sum(svc)
+    sec["amdahl"] = split
+    return sec
+
+
+def _arrivals(rate: float, seconds: float, seed: int):
+    import random
+
+    from d4gb import engine as E
+    from d4gb.problem import batched_instance
+
+    rng = random.Random(seed)
+    n = int(rate * seconds)
+    t, arr = 0.0, []
+    for _ in range(n):
+        t += rng.expovariate(rate)
+        arr.append(t)
+    probs = [batched_instance(rng, i) for i in range(n)]
+    modes = [E.MODE_SOLVE_ONE if rng.random() < 0.7 else E.MODE_COUNT for _ in range(n)]
+    return arr, probs, modes
+
+
+def _latency_summary(lat_done: list[float], cut: list[float]) -> dict:
+    """p50/p99 over every request: the unfinished ones count with the time
+    they had waited when the run was cut (a lower bound of their latency)."""
+    allv = lat_done + cut
+    return {"p50": _percentile(allv, 0.5), "p99": _percentile(allv, 0.99),
+            "p50_completed": _percentile(lat_done, 0.5),
+            "p99_completed": _percentile(lat_done, 0.99)}
+
+
+def serve_served(E, dev, arr, probs, modes, max_states, beam, grace: float) -> dict:
+    """The continuous-batching server under the arrival stream (open loop)."""
+    from d4gb.problem import verify_tiling
+
+    n = len(arr)
+    srv = E.Server(device=dev, max_states=max_states, beam=beam)
+    results = {}
+    t0 = time.perf_counter()
+    for i, (p, m, ta) in enumerate(zip(probs, modes, arr)):
+        while True:
+            now = time.perf_counter() - t0
+            if now >= ta:
+                break
+            for r in srv.poll():
+                results[r["tag"]] = r
+            time.sleep(min(ta - now, 0.0005))
+        srv.submit(p, m, i)
+    deadline = t0 + arr[-1] + grace
+    while len(results) < n and time.perf_counter() < deadline:
+        for r in srv.poll():
+            results[r["tag"]] = r
+        time.sleep(0.001)
+    elapsed = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    done = [r for r in results.values() if r["status"] == 0]
+    bad = sum(1 for r in done if r["found"] and
+              not verify_tiling(probs[r["tag"]], r["grid"], r["steps"]))
+    if bad:
+        raise RuntimeError(f"{bad} served solve-one tilings fail the cover check")
+    cut = [(elapsed - arr[i]) * 1e3 for i in range(n) if i not in results]
+    return {"completed": len(done), "failed": sum(1 for r in results.values() if r["status"]),
+            "unfinished": n - len(results), "elapsed_s": elapsed,
+            "puzzles_per_s": len(done) / elapsed,
+            "latency_ms": _latency_summary([r["latency_ms"] for r in done], cut),
+            "cover_checked": sum(1 for r in done if r["found"]),
+            "moved_to_slow_lane": st["moved"], "peak_active": st["peak_active"],
+            "results": {r["tag"]: (r["status"], r["count"], r["found"]) for r in results.values()}}
+
+
+def serve_plain(E, dev, arr, probs, modes, max_states, beam, grace: float) -> dict:
+    """The plain per-request path under the same arrivals, measured: one
+    request at a time in arrival order (FIFO), each through the engine alone
+    (d4e_batch_run with one instance)."""
+    n = len(arr)
+    lat, results = [], {}
+    t0 = time.perf_counter()
+    deadline = t0 + arr[-1] + grace
+    for i in range(n):
+        now = time.perf_counter() - t0
+        if now < arr[i]:
+            time.sleep(arr[i] - now)
+        if time.perf_counter() > deadline:
+            break
+        out, _ = E.batch_run([probs[i]], mode=modes[i], sequential=True, device=dev,
+                             max_states=max_states, beam=beam)
+        done = time.perf_counter() - t0
+        r = out[0]
+        results[i] = (r["status"], r["count"], r["found"])
+        if r["status"] == 0:
+            lat.append((done - arr[i]) * 1e3)
+    elapsed = time.perf_counter() - t0
+    cut = [(elapsed - arr[i]) * 1e3 for i in range(n) if i not in results]
+    return {"completed": len(lat), "unfinished": n - len(results), "elapsed_s": elapsed,
+            "puzzles_per_s": len(lat) / elapsed,
+            "latency_ms": _latency_summary(lat, cut), "results": results}
+
+
+def serve_section(E, dev: int, rate: float, seconds: float, max_states: int, beam: int,
+                  grace: float) -> dict:
+    """Config 5 (shortened): Poisson arrivals at `rate` for `seconds`, 70 %
+    solve-one / 30 % counting from the batched-mix distribution, through the
+    server and through the plain per-request path under the same arrivals;
+    every result of both arms compared."""
+    arr, probs, modes = _arrivals(rate, seconds, SERVE_SEED)
+    served = serve_served(E, dev, arr, probs, modes, max_states, beam, grace)
+    plain = serve_plain(E, dev, arr, probs, modes, max_states, beam, grace)
+    rs, rp = served.pop("results"), plain.pop("results")
+    for i in set(rs) & set(rp):
+        if rs[i][0] == 0 and rp[i][0] == 0 and rs[i] != rp[i]:
+            raise RuntimeError(f"request {i}: served and plain results differ")
+    return {"rate_req_s": rate, "arrival_window_s": seconds, "requests": len(arr),
+            "grace_s": grace, "served": served, "plain": plain,
+            "speedup_vs_plain": served["puzzles_per_s"] / plain["puzzles_per_s"]
+            if plain["puzzles_per_s"] else None}
 
 
 def main() -> None:

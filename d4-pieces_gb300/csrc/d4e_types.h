@@ -130,6 +130,7 @@ enum : uint32_t {
     kStatusTableOverflow = 1u,    // probe limit reached: table too small, level is redone
     kStatusNodeOverflow = 2u,     // solution path buffer full
     kStatusBucketOverflow = 4u,   // partitioned dedup: a bucket or its on-chip table was full
+    kStatusCompactStall = 8u,     // k_compact: a staged tile did not arrive in time (launch ended)
 };
 
 // Partitioned dedup: on-chip table slots per bucket (k_bucket_merge) and the

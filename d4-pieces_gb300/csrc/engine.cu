@@ -1200,6 +1200,7 @@ StepStats Engine::step_impl() {
         c.inst_off = inst_off_;
         c.inst_mask = inst_mask_;
         c.keep_max = sampled.empty() ? nullptr : keep_max_.p;
+        c.status = misc_.p;
         const int cgrid = compact_grid(ccap, sms_);
         phase(tot_.ph_post_ms);
         cuda_check(cudaEventRecord(ev_[2], stream_), "cudaEventRecord");
@@ -1208,7 +1209,13 @@ StepStats Engine::step_impl() {
         cuda_check(cudaEventRecord(ev_[3], stream_), "cudaEventRecord");
         tot_.compact_launches++;
         tot_.compact_slots += ccap;
+        unsigned int c_status = 0;
+        cuda_check(cudaMemcpyAsync(&c_status, misc_.p, sizeof(unsigned int),
+                                   cudaMemcpyDeviceToHost, stream_),
+                   "read status");
         cuda_check(cudaStreamSynchronize(stream_), "k_compact");
+        if (c_status & kStatusCompactStall)
+            throw Error(kErrCuda, "k_compact: a staged table tile did not arrive");
         phase(tot_.ph_compact_ms);
         float cms = 0.f;
         cudaEventElapsedTime(&cms, ev_[2], ev_[3]);
@@ -1554,6 +1561,7 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
         c.inst_off = inst_off_;
         c.inst_mask = inst_mask_;
         c.keep_max = nullptr;
+        c.status = misc_.p;
         const int cgrid = compact_grid(cap, sms_);
         cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
         launch_expand(k64_, a, grid, stream_);
@@ -1569,6 +1577,8 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
         cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
         for (uint32_t id : grp)
             inst_[id].min_region = 0;
+        if (stt & kStatusCompactStall)
+            throw Error(kErrCuda, "k_compact: a staged table tile did not arrive");
         return (stt & kStatusTableOverflow) ? 1e30 : (double)ms;
     };
     Tuning best = tune_;

@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 
 #include "state_hash.cuh"
 
@@ -720,44 +722,397 @@ k_expand(ExpandArgs a) {
         atomicAdd(a.n_raw, tot);
 }
 
-// Compaction works on tiles of kCompactPer x 256 slots per block iteration
-// (slot tile_base + j * 256 + thread for round j).  When every occupied slot
-// of the tile belongs to one instance -- always for a single puzzle -- the
-// block computes output positions with ballots and one shared prefix and
-// reserves them with ONE cursor atomic per tile, writing coalesced runs.
-// Tiles holding several instances (batches) reserve per round and warp with
-// __match_any_sync aggregation instead.
-constexpr int kCompactPer = 8;
+// Compaction streams the table in tiles of kCompactTileBytes (2048 K64 or
+// 1024 K128 slots; slot tile_base + j * kCompactBlock + thread for round j).
+// The tiles come into shared memory by 1-D bulk copies (cp.async.bulk, the
+// async copy engine), kCompactStages deep per block, so every block keeps
+// ~64 KB of the table in flight while it works on the tile it holds.  When
+// every occupied slot of a tile belongs to one instance -- always for a
+// single puzzle, and for every tile of a batch, whose instances own whole
+// tiles -- the block computes output positions with ballots and one shared
+// prefix and reserves them with ONE cursor atomic per tile, writing
+// coalesced runs.  Tiles holding several instances reserve per round and warp
+// with __match_any_sync aggregation instead.  Occupied slots are cleared in
+// the table as they are taken.
+constexpr int kCompactTileBytes = 32768;
+constexpr int kCompactStages = 3;
 constexpr int kCompactWarps = kCompactBlock / 32;
+constexpr int kCompactSmem = kCompactTileBytes * kCompactStages;
+// A staged tile that has not arrived after this long (never expected: the
+// copy engine reads device memory the kernel owns) ends the launch with
+// kStatusCompactStall instead of waiting on.
+constexpr unsigned long long kCompactWaitNs = 2000000000ull;
 
 template <bool K64>
-__global__ void __launch_bounds__(kCompactBlock)
-k_compact(CompactArgs a) {
-    __shared__ unsigned int s_cnt[kCompactPer][kCompactWarps];   // stored slots per round, warp
-    __shared__ uint32_t s_min[kCompactWarps], s_max[kCompactWarps];
-    __shared__ unsigned long long s_base, s_fin_sum;
-    __shared__ unsigned int s_fin_n;
+__host__ __device__ constexpr int compact_per() {
+    return kCompactTileBytes / (K64 ? 16 : 32) / kCompactBlock;
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+
+// Arms the barrier for `bytes` of transfer (and the issuing thread's arrival).
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0u;
+}
+
+// Waits for phase `parity` of the barrier for at most kCompactWaitNs;
+// false on a timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity))
+        return true;
+    const unsigned long long t0 = global_ns();
+    for (;;) {
+        if (mbar_try_wait(bar, parity))
+            return true;
+        if (global_ns() - t0 > kCompactWaitNs)
+            return false;
+    }
+}
+
+// Global -> shared bulk copy completing on `bar` (both addresses 16-byte
+// aligned, bytes a multiple of 16).
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes,
+                                          unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// Orders this thread's earlier shared-memory accesses before later
+// async-proxy (bulk copy) accesses of the same memory.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Shared bookkeeping of one k_compact block.
+template <int PER>
+struct CompactShared {
+    unsigned int cnt[PER][kCompactWarps];   // stored slots per round, warp
+    uint32_t min[kCompactWarps], max[kCompactWarps];
+    unsigned long long base, fin_sum;
+    unsigned int fin_n;
+};
+
+// Moves one tile's occupied slots (already in registers: key words, value,
+// instance id or 0xFFFFFFFF for an empty slot) to their instances' next
+// frontier segments or final results.  Every thread of the block calls it.
+template <bool K64, int PER>
+__device__ __forceinline__ void compact_tile(const CompactArgs &a, CompactShared<PER> &sh,
+                                             const unsigned long long (&k0)[PER],
+                                             const unsigned long long (&k1)[PER],
+                                             const unsigned long long (&cnt)[PER],
+                                             const uint32_t (&inst)[PER]) {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
-    const unsigned long long tile = (unsigned long long)kCompactPer * kCompactBlock;
-    for (unsigned long long tb = (unsigned long long)blockIdx.x * tile; tb < a.cap;
-         tb += (unsigned long long)gridDim.x * tile) {
-        unsigned long long k0[kCompactPer], k1[kCompactPer], cnt[kCompactPer];
-        uint32_t inst[kCompactPer];
-        uint32_t tmin = 0xFFFFFFFFu, tmax = 0u;
+    uint32_t tmin = 0xFFFFFFFFu, tmax = 0u;
 #pragma unroll
-        for (int j = 0; j < kCompactPer; j++) {
+    for (int j = 0; j < PER; j++)
+        if (inst[j] != 0xFFFFFFFFu) {
+            tmin = min(tmin, inst[j]);
+            tmax = max(tmax, inst[j]);
+        }
+    // Is the tile single-instance?
+    for (int o = 16; o > 0; o >>= 1) {
+        tmin = min(tmin, __shfl_xor_sync(0xffffffffu, tmin, o));
+        tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+    }
+    if (lane == 0) {
+        sh.min[warp] = tmin;
+        sh.max[warp] = tmax;
+    }
+    __syncthreads();
+    uint32_t bmin = 0xFFFFFFFFu, bmax = 0u;
+#pragma unroll
+    for (int w = 0; w < kCompactWarps; w++) {
+        bmin = min(bmin, sh.min[w]);
+        bmax = max(bmax, sh.max[w]);
+    }
+    if (bmin == 0xFFFFFFFFu) {   // empty tile
+        __syncthreads();
+        return;
+    }
+    if (bmin == bmax) {
+        // ---- single instance: one reservation for the tile -----------------
+        const uint32_t in0 = bmin;
+        const unsigned long long cur = a.cursor[in0];
+        const bool fin = cur == kCursorFinal;
+        const bool drop = cur == kCursorDrop;
+        const unsigned long long km = a.keep_max ? a.keep_max[in0] : ~0ull;
+        bool st[PER];
+        unsigned long long fsum = 0;
+        unsigned int fn = 0;
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            const bool occ = inst[j] != 0xFFFFFFFFu;
+            st[j] = occ && !fin && !drop;
+            if (st[j] && km != ~0ull) {
+                const unsigned long long wid =
+                    K64 ? (k0[j] & ((1ull << a.inst_off) - 1ull)) : witness128(k0[j], k1[j]);
+                st[j] = sample_hash(wid) <= km;
+            }
+            if (occ && fin) {
+                fsum += cnt[j];
+                fn++;
+            }
+            const unsigned b = __ballot_sync(0xffffffffu, st[j]);
+            if (lane == 0)
+                sh.cnt[j][warp] = __popc(b);
+        }
+        if (fin) {
+            for (int o = 16; o > 0; o >>= 1) {
+                fsum += __shfl_xor_sync(0xffffffffu, fsum, o);
+                fn += __shfl_xor_sync(0xffffffffu, fn, o);
+            }
+            if (threadIdx.x == 0) {
+                sh.fin_sum = 0;
+                sh.fin_n = 0;
+            }
+        }
+        __syncthreads();
+        if (fin) {
+            if (lane == 0 && fn) {
+                atomicAdd(&sh.fin_sum, fsum);
+                atomicAdd(&sh.fin_n, fn);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0 && sh.fin_n) {
+                atomicAdd(&a.results[in0], sh.fin_sum);
+                atomicAdd(&a.final_states[in0], sh.fin_n);
+            }
+            __syncthreads();
+            return;
+        }
+        if (threadIdx.x == 0) {
+            unsigned int total = 0;
+            for (int j = 0; j < PER; j++)
+                for (int w = 0; w < kCompactWarps; w++)
+                    total += sh.cnt[j][w];
+            sh.base = total ? atomicAdd(&a.cursor[in0], (unsigned long long)total) : 0ull;
+        }
+        __syncthreads();
+        // Position = base + stored slots before (round j, warp, lane).
+        unsigned long long pos = sh.base;
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            unsigned int before = 0, round_total = 0;
+#pragma unroll
+            for (int w = 0; w < kCompactWarps; w++) {
+                before += w < (int)warp ? sh.cnt[j][w] : 0u;
+                round_total += sh.cnt[j][w];
+            }
+            const unsigned b = __ballot_sync(0xffffffffu, st[j]);
+            if (st[j]) {
+                const unsigned long long p = pos + before + __popc(b & lt);
+                if constexpr (K64) {
+                    a.out_recs[p] = make_ulonglong2(k0[j], cnt[j]);
+                } else {
+                    a.out_recs[p] = make_ulonglong2(k0[j], k1[j]);
+                    a.out_cnts[p] = cnt[j];
+                }
+            }
+            pos += round_total;
+        }
+        __syncthreads();
+        return;
+    }
+    // ---- several instances: warp-aggregated reservation per round ----------
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        const bool occ = inst[j] != 0xFFFFFFFFu;
+        const unsigned long long cur = occ ? a.cursor[inst[j]] : 0ull;
+        const bool fin = occ && cur == kCursorFinal;
+        bool store = occ && !fin && cur != kCursorDrop;
+        if (store && a.keep_max) {
+            const unsigned long long km = a.keep_max[inst[j]];
+            if (km != ~0ull) {
+                const unsigned long long wid =
+                    K64 ? (k0[j] & ((1ull << a.inst_off) - 1ull)) : witness128(k0[j], k1[j]);
+                store = sample_hash(wid) <= km;
+            }
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, store ? inst[j] : 0xFFFFFFFFu);
+        if (store) {
+            const unsigned leader = __ffs(peers) - 1;
+            unsigned long long basepos = 0;
+            if (lane == leader)
+                basepos = atomicAdd(&a.cursor[inst[j]], (unsigned long long)__popc(peers));
+            basepos = __shfl_sync(peers, basepos, leader);
+            const unsigned long long p = basepos + __popc(peers & lt);
+            if constexpr (K64) {
+                a.out_recs[p] = make_ulonglong2(k0[j], cnt[j]);
+            } else {
+                a.out_recs[p] = make_ulonglong2(k0[j], k1[j]);
+                a.out_cnts[p] = cnt[j];
+            }
+        }
+        if (fin) {
+            atomicAdd(&a.results[inst[j]], cnt[j]);
+            atomicAdd(&a.final_states[inst[j]], 1u);
+        }
+    }
+    __syncthreads();
+}
+
+// Reads slot i of a staged tile (shared memory) into registers; returns the
+// instance id, or 0xFFFFFFFF for an empty slot.
+template <bool K64>
+__device__ __forceinline__ uint32_t read_slot(const CompactArgs &a, const unsigned char *tile,
+                                              uint32_t i, unsigned long long &k0,
+                                              unsigned long long &k1, unsigned long long &cnt) {
+    if constexpr (K64) {
+        const ulonglong2 v = reinterpret_cast<const ulonglong2 *>(tile)[i];
+        k0 = v.x;
+        k1 = 0;
+        cnt = v.y;
+        return v.x ? (uint32_t)((v.x >> a.inst_off) & a.inst_mask) : 0xFFFFFFFFu;
+    } else {
+        const ulonglong2 v = reinterpret_cast<const ulonglong2 *>(tile)[2 * i];
+        k0 = v.x;
+        k1 = v.y;
+        cnt = reinterpret_cast<const unsigned long long *>(tile)[4 * i + 2];
+        return v.y ? (uint32_t)((v.y & ~kMarker) >> kInstShift128) : 0xFFFFFFFFu;
+    }
+}
+
+template <bool K64>
+__global__ void __launch_bounds__(kCompactBlock, 2)
+k_compact(CompactArgs a) {
+    constexpr int PER = compact_per<K64>();
+    constexpr uint32_t kSlotBytes = K64 ? 16u : 32u;
+    constexpr unsigned long long kTile = (unsigned long long)PER * kCompactBlock;   // slots
+    extern __shared__ __align__(128) unsigned char c_stage[];
+    __shared__ __align__(8) unsigned long long bars[kCompactStages];
+    __shared__ CompactShared<PER> sh;
+    const unsigned long long n_tiles = (a.cap + kTile - 1) / kTile;
+    const unsigned long long mine =
+        blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0ull;
+    // Thread 0 issues the bulk copy of this block's k-th tile into stage k % S.
+    auto issue = [&](unsigned long long k) {
+        const unsigned long long first = (blockIdx.x + k * gridDim.x) * kTile;
+        const unsigned long long n = a.cap - first < kTile ? a.cap - first : kTile;
+        unsigned long long *bar = &bars[k % kCompactStages];
+        const uint32_t bytes = (uint32_t)n * kSlotBytes;
+        mbar_expect_tx(bar, bytes);
+        bulk_load(c_stage + (k % kCompactStages) * kCompactTileBytes,
+                  static_cast<const unsigned char *>(a.table) + first * kSlotBytes, bytes, bar);
+    };
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kCompactStages; s++)
+            mbar_init(&bars[s], 1);
+        fence_mbar_init();
+        fence_proxy_async_smem();
+        for (unsigned long long k = 0; k < mine && k < (unsigned long long)kCompactStages; k++)
+            issue(k);
+    }
+    __syncthreads();
+    unsigned long long k = 0;
+    for (; k < mine; k++) {
+        const int s = (int)(k % kCompactStages);
+        const uint32_t parity = (uint32_t)((k / kCompactStages) & 1ull);
+        const bool ok = mbar_wait_bounded(&bars[s], parity);
+        if (__syncthreads_or(!ok))
+            break;
+        const unsigned long long tb = (blockIdx.x + k * gridDim.x) * kTile;
+        const unsigned char *tile = c_stage + s * kCompactTileBytes;
+        unsigned long long k0[PER], k1[PER], cnt[PER];
+        uint32_t inst[PER];
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            const uint32_t i = (uint32_t)j * kCompactBlock + threadIdx.x;
+            inst[j] = 0xFFFFFFFFu;
+            k0[j] = k1[j] = cnt[j] = 0;
+            if (tb + i < a.cap)
+                inst[j] = read_slot<K64>(a, tile, i, k0[j], k1[j], cnt[j]);
+        }
+        // Every thread has read the stage: refill it with tile k + S.
+        __syncthreads();
+        if (threadIdx.x == 0 && k + kCompactStages < mine) {
+            fence_proxy_async_smem();
+            issue(k + kCompactStages);
+        }
+        // Clear the taken slots for the next row.
+#pragma unroll
+        for (int j = 0; j < PER; j++)
+            if (inst[j] != 0xFFFFFFFFu) {
+                const unsigned long long i = tb + (unsigned long long)j * kCompactBlock + threadIdx.x;
+                if constexpr (K64)
+                    static_cast<ulonglong2 *>(a.table)[i] = make_ulonglong2(0, 0);
+                else
+                    static_cast<ulonglong4_32a *>(a.table)[i] = make_ulonglong4_32a(0, 0, 0, 0);
+            }
+        compact_tile<K64, PER>(a, sh, k0, k1, cnt, inst);
+    }
+    if (k < mine) {
+        // A stage that did not arrive: report it, and let the copies still
+        // in flight land (each wait bounded) before the block's shared memory
+        // is given up.
+        if (threadIdx.x == 0) {
+            atomicOr(a.status, kStatusCompactStall);
+            const unsigned long long last = mine < k + kCompactStages ? mine : k + kCompactStages;
+            for (unsigned long long q = k; q < last; q++)
+                mbar_wait_bounded(&bars[q % kCompactStages],
+                                  (uint32_t)((q / kCompactStages) & 1ull));
+        }
+        __syncthreads();
+    }
+}
+
+// Loads a tile straight into registers (no staging): the variant the staged
+// kernel is measured against (D4E_COMPACT=ld).
+template <bool K64>
+__global__ void __launch_bounds__(kCompactBlock)
+k_compact_ld(CompactArgs a) {
+    constexpr int PER = compact_per<K64>();
+    constexpr unsigned long long kTile = (unsigned long long)PER * kCompactBlock;
+    __shared__ CompactShared<PER> sh;
+    for (unsigned long long tb = (unsigned long long)blockIdx.x * kTile; tb < a.cap;
+         tb += (unsigned long long)gridDim.x * kTile) {
+        unsigned long long k0[PER], k1[PER], cnt[PER];
+        uint32_t inst[PER];
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
             const unsigned long long i = tb + (unsigned long long)j * kCompactBlock + threadIdx.x;
             k0[j] = k1[j] = cnt[j] = 0;
             inst[j] = 0xFFFFFFFFu;
             if (i < a.cap) {
-                bool occ;
                 if constexpr (K64) {
                     const ulonglong2 v = static_cast<const ulonglong2 *>(a.table)[i];
                     k0[j] = v.x;
                     cnt[j] = v.y;
-                    occ = v.x != 0ull;
-                    if (occ) {
+                    if (v.x) {
                         inst[j] = (uint32_t)((v.x >> a.inst_off) & a.inst_mask);
                         static_cast<ulonglong2 *>(a.table)[i] = make_ulonglong2(0, 0);
                     }
@@ -766,159 +1121,15 @@ k_compact(CompactArgs a) {
                     k0[j] = v.x;
                     k1[j] = v.y;
                     cnt[j] = v.z;
-                    occ = v.y != 0ull;
-                    if (occ) {
+                    if (v.y) {
                         inst[j] = (uint32_t)((v.y & ~kMarker) >> kInstShift128);
                         static_cast<ulonglong4_32a *>(a.table)[i] =
                             make_ulonglong4_32a(0, 0, 0, 0);
                     }
                 }
-                if (occ) {
-                    tmin = min(tmin, inst[j]);
-                    tmax = max(tmax, inst[j]);
-                }
             }
         }
-        // Is the tile single-instance?
-        for (int o = 16; o > 0; o >>= 1) {
-            tmin = min(tmin, __shfl_xor_sync(0xffffffffu, tmin, o));
-            tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
-        }
-        if (lane == 0) {
-            s_min[warp] = tmin;
-            s_max[warp] = tmax;
-        }
-        __syncthreads();
-        uint32_t bmin = 0xFFFFFFFFu, bmax = 0u;
-#pragma unroll
-        for (int w = 0; w < kCompactWarps; w++) {
-            bmin = min(bmin, s_min[w]);
-            bmax = max(bmax, s_max[w]);
-        }
-        if (bmin == 0xFFFFFFFFu) {   // empty tile
-            __syncthreads();
-            continue;
-        }
-        if (bmin == bmax) {
-            // ---- single instance: one reservation for the tile -------------
-            const uint32_t in0 = bmin;
-            const unsigned long long cur = a.cursor[in0];
-            const bool fin = cur == kCursorFinal;
-            const bool drop = cur == kCursorDrop;
-            const unsigned long long km = a.keep_max ? a.keep_max[in0] : ~0ull;
-            bool st[kCompactPer];
-            unsigned long long fsum = 0;
-            unsigned int fn = 0;
-#pragma unroll
-            for (int j = 0; j < kCompactPer; j++) {
-                const bool occ = inst[j] != 0xFFFFFFFFu;
-                st[j] = occ && !fin && !drop;
-                if (st[j] && km != ~0ull) {
-                    const unsigned long long wid =
-                        K64 ? (k0[j] & ((1ull << a.inst_off) - 1ull)) : witness128(k0[j], k1[j]);
-                    st[j] = sample_hash(wid) <= km;
-                }
-                if (occ && fin) {
-                    fsum += cnt[j];
-                    fn++;
-                }
-                const unsigned b = __ballot_sync(0xffffffffu, st[j]);
-                if (lane == 0)
-                    s_cnt[j][warp] = __popc(b);
-            }
-            if (fin) {
-                for (int o = 16; o > 0; o >>= 1) {
-                    fsum += __shfl_xor_sync(0xffffffffu, fsum, o);
-                    fn += __shfl_xor_sync(0xffffffffu, fn, o);
-                }
-                if (threadIdx.x == 0) {
-                    s_fin_sum = 0;
-                    s_fin_n = 0;
-                }
-            }
-            __syncthreads();
-            if (fin) {
-                if (lane == 0 && fn) {
-                    atomicAdd(&s_fin_sum, fsum);
-                    atomicAdd(&s_fin_n, fn);
-                }
-                __syncthreads();
-                if (threadIdx.x == 0 && s_fin_n) {
-                    atomicAdd(&a.results[in0], s_fin_sum);
-                    atomicAdd(&a.final_states[in0], s_fin_n);
-                }
-                __syncthreads();
-                continue;
-            }
-            if (threadIdx.x == 0) {
-                unsigned int total = 0;
-                for (int j = 0; j < kCompactPer; j++)
-                    for (int w = 0; w < kCompactWarps; w++)
-                        total += s_cnt[j][w];
-                s_base = total ? atomicAdd(&a.cursor[in0], (unsigned long long)total) : 0ull;
-            }
-            __syncthreads();
-            // Position = base + stored slots before (round j, warp, lane).
-            unsigned long long pos = s_base;
-#pragma unroll
-            for (int j = 0; j < kCompactPer; j++) {
-                unsigned int before = 0;
-                for (int w = 0; w < kCompactWarps; w++)
-                    before += w < (int)warp ? s_cnt[j][w] : 0u;
-                const unsigned b = __ballot_sync(0xffffffffu, st[j]);
-                if (st[j]) {
-                    const unsigned long long p = pos + before + __popc(b & lt);
-                    if constexpr (K64) {
-                        a.out_recs[p] = make_ulonglong2(k0[j], cnt[j]);
-                    } else {
-                        a.out_recs[p] = make_ulonglong2(k0[j], k1[j]);
-                        a.out_cnts[p] = cnt[j];
-                    }
-                }
-                unsigned int round_total = 0;
-                for (int w = 0; w < kCompactWarps; w++)
-                    round_total += s_cnt[j][w];
-                pos += round_total;
-            }
-            __syncthreads();
-            continue;
-        }
-        // ---- several instances: warp-aggregated reservation per round ------
-#pragma unroll
-        for (int j = 0; j < kCompactPer; j++) {
-            const bool occ = inst[j] != 0xFFFFFFFFu;
-            const unsigned long long cur = occ ? a.cursor[inst[j]] : 0ull;
-            const bool fin = occ && cur == kCursorFinal;
-            bool store = occ && !fin && cur != kCursorDrop;
-            if (store && a.keep_max) {
-                const unsigned long long km = a.keep_max[inst[j]];
-                if (km != ~0ull) {
-                    const unsigned long long wid =
-                        K64 ? (k0[j] & ((1ull << a.inst_off) - 1ull)) : witness128(k0[j], k1[j]);
-                    store = sample_hash(wid) <= km;
-                }
-            }
-            const unsigned peers = __match_any_sync(0xffffffffu, store ? inst[j] : 0xFFFFFFFFu);
-            if (store) {
-                const unsigned leader = __ffs(peers) - 1;
-                unsigned long long basepos = 0;
-                if (lane == leader)
-                    basepos = atomicAdd(&a.cursor[inst[j]], (unsigned long long)__popc(peers));
-                basepos = __shfl_sync(peers, basepos, leader);
-                const unsigned long long p = basepos + __popc(peers & lt);
-                if constexpr (K64) {
-                    a.out_recs[p] = make_ulonglong2(k0[j], cnt[j]);
-                } else {
-                    a.out_recs[p] = make_ulonglong2(k0[j], k1[j]);
-                    a.out_cnts[p] = cnt[j];
-                }
-            }
-            if (fin) {
-                atomicAdd(&a.results[inst[j]], cnt[j]);
-                atomicAdd(&a.final_states[inst[j]], 1u);
-            }
-        }
-        __syncthreads();
+        compact_tile<K64, PER>(a, sh, k0, k1, cnt, inst);
     }
 }
 
@@ -1144,20 +1355,46 @@ void launch_expand(bool k64, const ExpandArgs &a, int grid, cudaStream_t s) {
         k_expand<false><<<grid, kExpandBlock, 0, s>>>(a);
 }
 
+namespace {
+// D4E_COMPACT=ld selects the unstaged compaction (for measurements).
+bool compact_unstaged() {
+    static const bool ld = [] {
+        const char *v = std::getenv("D4E_COMPACT");
+        return v && std::strcmp(v, "ld") == 0;
+    }();
+    return ld;
+}
+}  // namespace
+
 int compact_grid(unsigned long long cap, int sms) {
-    const unsigned long long tile = (unsigned long long)kCompactPer * kCompactBlock;
-    const unsigned long long tiles = (cap + tile - 1) / tile;
-    return (int)std::max<unsigned long long>(1ull, std::min<unsigned long long>(tiles,
-                                                                              (unsigned long long)sms * 8));
+    // Tiles of 32 KB (2048 K64 or 1024 K128 slots; the smaller count bounds
+    // the grid either way).
+    const unsigned long long tiles = (cap + 1023) / 1024;
+    const unsigned long long per_sm = compact_unstaged() ? 8ull : 2ull;
+    return (int)std::max<unsigned long long>(
+        1ull, std::min<unsigned long long>(tiles, (unsigned long long)sms * per_sm));
 }
 
 void launch_compact(bool k64, const CompactArgs &a, int grid, cudaStream_t s) {
     if (a.cap == 0)
         return;
-    if (k64)
-        k_compact<true><<<grid, kCompactBlock, 0, s>>>(a);
-    else
-        k_compact<false><<<grid, kCompactBlock, 0, s>>>(a);
+    if (compact_unstaged()) {
+        if (k64)
+            k_compact_ld<true><<<grid, kCompactBlock, 0, s>>>(a);
+        else
+            k_compact_ld<false><<<grid, kCompactBlock, 0, s>>>(a);
+        return;
+    }
+    // The staging ring is dynamic shared memory beyond the default 48 KB.
+    if (k64) {
+        cudaFuncSetAttribute(k_compact<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kCompactSmem);
+        k_compact<true><<<grid, kCompactBlock, kCompactSmem, s>>>(a);
+    } else {
+        cudaFuncSetAttribute(k_compact<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kCompactSmem);
+        k_compact<false><<<grid, kCompactBlock, kCompactSmem, s>>>(a);
+    }
 }
 
 void launch_keyset_insert(bool k64, const KeySetArgs &t, const ulonglong2 *recs,

@@ -74,6 +74,7 @@ struct CompactArgs {
     // Per instance: keep a state only if its sample hash is <= keep_max
     // (~0 = keep all).  nullptr = no sampling.
     const unsigned long long *keep_max;
+    unsigned int *status;            // kStatusCompactStall is or'ed in here
 };
 
 // Resident k_expand blocks per SM (for sizing its persistent grid).
@@ -88,8 +89,8 @@ void launch_expand(bool k64, const ExpandArgs &a, int grid, cudaStream_t s);
 // the table.
 void launch_compact(bool k64, const CompactArgs &a, int grid, cudaStream_t s);
 
-// k_compact grid for a table of `cap` slots (tiles of 2048 slots, at most
-// 8 blocks per SM).
+// k_compact grid for a table of `cap` slots (32 KB tiles, two blocks per SM,
+// each streaming its tiles through a shared-memory ring).
 int compact_grid(unsigned long long cap, int sms);
 
 // Solution reconstruction -------------------------------------------------

@@ -294,6 +294,7 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
             c.final_states = d_final;
             c.inst_off = lib.dyn_bits + lib.used_bits;
             c.inst_mask = 0;
+            c.status = d_status;
             launch_compact(k64, c, compact_grid(L.cap_slots, sms), s);
             cuda_check(cudaGetLastError(), "k_compact launch");
             if (last) {
@@ -301,7 +302,13 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
                                            cudaMemcpyDeviceToHost, s),
                            "read result");
             }
+            unsigned int c_status = 0;
+            cuda_check(cudaMemcpyAsync(&c_status, d_status, sizeof(c_status),
+                                       cudaMemcpyDeviceToHost, s),
+                       "read status");
             cuda_check(cudaStreamSynchronize(s), "k_compact");
+            if (c_status & kStatusCompactStall)
+                return abi_fail(D4E_ERR_CUDA, "k_compact: a staged table tile did not arrive");
             total_states += uniq;
             n = uniq;
             cur = 1 - cur;

@@ -860,8 +860,9 @@ static void *lean_collect_run(void *arg)
     return NULL;
 }
 
-int32_t or_rowdp_lean(const or_problem *p, int32_t threads, uint64_t *level_sizes,
-                      uint64_t *raw_sizes, uint64_t *count, double *seconds)
+int32_t or_rowdp_lean(const or_problem *p, int32_t threads, int32_t max_rows,
+                      uint64_t *level_sizes, uint64_t *raw_sizes, uint64_t *count,
+                      double *seconds)
 {
     or_ctx c;
     if (build_ctx(p, &c))
@@ -894,7 +895,8 @@ int32_t or_rowdp_lean(const or_problem *p, int32_t threads, uint64_t *level_size
     cur[0].used = 0;
     cur[0].cnt = 1;
     int32_t rc = 0;
-    for (int r = 0; r < c.H; r++) {
+    const int rows = (max_rows > 0 && max_rows < c.H) ? max_rows : c.H;
+    for (int r = 0; r < rows; r++) {
         size_t next = 0;
         for (int k = 0; k < T; k++) {
             ws[k].tab = &tab;
@@ -941,7 +943,7 @@ int32_t or_rowdp_lean(const or_problem *p, int32_t threads, uint64_t *level_size
             raw_sizes[r] = raw;
     }
     uint64_t cnt = 0;
-    if (rc == 0)
+    if (rc == 0 && rows == c.H)
         for (size_t i = 0; i < n_cur; i++)
             cnt += cur[i].cnt;
     if (count)

@@ -86,11 +86,13 @@ int32_t or_rowdp(const or_problem *p, int32_t threads, double max_seconds,
  * first, so memory holds each level's distinct states only (32 bytes each,
  * plus the shards' free slots).  level_sizes[r] = distinct states after
  * row r, raw_sizes[r] = children produced while completing row r (either
- * may be NULL); *count = tilings (mod 2^64); *seconds = elapsed time.
- * Runs every row to the end.  Returns 0, -1 on bad input, -2 when host
- * memory ran out. */
-int32_t or_rowdp_lean(const or_problem *p, int32_t threads, uint64_t *level_sizes,
-                      uint64_t *raw_sizes, uint64_t *count, double *seconds);
+ * may be NULL); *count = tilings (mod 2^64; 0 unless every row ran);
+ * *seconds = elapsed time.  max_rows > 0 stops after that many whole rows
+ * (a timed sample of the first rows), otherwise every row runs.  Returns 0,
+ * -1 on bad input, -2 when host memory ran out. */
+int32_t or_rowdp_lean(const or_problem *p, int32_t threads, int32_t max_rows,
+                      uint64_t *level_sizes, uint64_t *raw_sizes, uint64_t *count,
+                      double *seconds);
 
 /* Independent cover check of one tiling given as placements:
  * piece type + cell mask (lo/hi 64-bit halves of the W-stride bitboard).

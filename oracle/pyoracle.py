@@ -59,9 +59,9 @@ def _load():
                                  C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_uint64)]
         lib.or_rowdp_lean.restype = C.c_int32
-        lib.or_rowdp_lean.argtypes = [C.POINTER(_Problem), C.c_int32, C.POINTER(C.c_uint64),
+        lib.or_rowdp_lean.argtypes = [C.POINTER(_Problem), C.c_int32, C.c_int32,
                                       C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
-                                      C.POINTER(C.c_double)]
+                                      C.POINTER(C.c_uint64), C.POINTER(C.c_double)]
         lib.or_check_tiling.restype = C.c_int32
         lib.or_check_tiling.argtypes = [C.POINTER(_Problem), C.c_int32, C.POINTER(C.c_int32),
                                         C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
@@ -131,19 +131,21 @@ def rowdp(p, threads: int = 1, max_seconds: float = 0.0, max_children: int = 0) 
             "levels_done": done.value, "states_total": int(total.value)}
 
 
-def rowdp_lean(p, threads: int = 1) -> dict:
+def rowdp_lean(p, threads: int = 1, max_rows: int = 0) -> dict:
     """Exact row DP de-duplicating children as they are produced (memory =
-    distinct states only); every row runs to the end."""
+    distinct states only); max_rows > 0 runs only the first whole rows."""
     st, keep = _prob(p)
     sizes = (C.c_uint64 * max(p.height, 1))()
     raw = (C.c_uint64 * max(p.height, 1))()
     count = C.c_uint64()
     secs = C.c_double()
-    r = _load().or_rowdp_lean(C.byref(st), threads, sizes, raw, C.byref(count), C.byref(secs))
+    r = _load().or_rowdp_lean(C.byref(st), threads, max_rows, sizes, raw, C.byref(count),
+                              C.byref(secs))
     if r != 0:
         raise ValueError("oracle rejected the problem" if r == -1 else "host memory ran out")
-    return {"level_sizes": list(sizes)[: p.height], "raw_sizes": list(raw)[: p.height],
-            "count": int(count.value), "seconds": secs.value}
+    rows = min(max_rows, p.height) if max_rows > 0 else p.height
+    return {"level_sizes": list(sizes)[:rows], "raw_sizes": list(raw)[:rows],
+            "count": int(count.value), "seconds": secs.value, "rows": rows}
 
 
 def check_tiling(p, types, masks) -> bool:
