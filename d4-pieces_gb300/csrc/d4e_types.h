@@ -39,12 +39,19 @@ constexpr uint64_t kMarker = 1ull << 63;
 constexpr uint64_t kUsedMask128 = (1ull << kInstShift128) - 1;
 
 // One placement anchored at a column of the current row: its cells in window
-// coordinates (bit i*W + c) and its piece type.
+// coordinates (bit i*W + c), its piece type, and that type's copy counter
+// (bits off .. off + bits - 1 of `used`; a copy is free while the field is
+// below count, and taking one adds 1 << off), so that the walk tests and
+// takes a copy without another load.
 struct Plc {
     uint64_t mask;
-    uint32_t type;
-    uint32_t next_type;   // column-relative index of the first placement of the next type
+    uint8_t type;
+    uint8_t next_type;    // column-relative index of the first placement of the next type
+    uint8_t off;
+    uint8_t bits;
+    uint32_t count;
 };
+static_assert(sizeof(Plc) == 16, "placement record");
 
 // Copy counter of one piece type: field mask and capacity (count << offset),
 // both in `used` coordinates.  A copy is available when (used & fm) < cap;

@@ -7,6 +7,7 @@
 #include <mutex>
 #include <map>
 #include <functional>
+#include <cstdlib>
 #include <cstring>
 
 #include "kernels.h"
@@ -594,6 +595,20 @@ uint64_t Engine::table_limit() {
     return std::max<uint64_t>(limit / kRegionAlign * kRegionAlign, kRegionAlign);
 }
 
+// Placements to stage in shared memory for a launch over `segs`: the
+// instance's whole table when the launch holds one instance and it fits
+// (D4E_STAGE_PLC=0 reads it through L1 instead).
+uint32_t Engine::stage_plc(const std::vector<Seg> &segs) const {
+    static const bool off = [] {
+        const char *v = std::getenv("D4E_STAGE_PLC");
+        return v && std::strcmp(v, "0") == 0;
+    }();
+    if (off || segs.size() != 1)
+        return 0;
+    const uint32_t np = inst_[segs[0].inst].desc.n_plc;
+    return expand_stage_bytes(np) <= kStageMaxBytes ? np : 0;
+}
+
 int Engine::expand_occupancy() {
     int &occ = k64_ ? occ64_ : occ128_;
     if (!occ) {
@@ -1054,6 +1069,7 @@ StepStats Engine::step_impl() {
         a.work = nraw_.p + 1;
         a.max_probe = opts_.max_probe;
         a.prefetch = units * sizeof(ulonglong2) <= kPrefetchTableBytes ? 1u : 0u;
+        a.stage_plc = stage_plc(segs);
         cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
         launch_expand(k64_, a, grid, stream_);
         cuda_check(cudaGetLastError(), "k_expand launch");
@@ -1550,6 +1566,7 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
         a.work = nraw_.p + 1;
         a.max_probe = opts_.max_probe;
         a.prefetch = units * sizeof(ulonglong2) <= kPrefetchTableBytes ? 1u : 0u;
+        a.stage_plc = stage_plc(segs);
         CompactArgs c{};
         c.table = table_.p;
         c.cap = cap;

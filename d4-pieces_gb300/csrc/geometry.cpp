@@ -228,7 +228,14 @@ std::string build_piece_lib(const uint64_t *shapes, const uint32_t *counts, uint
             uint64_t m = 0;
             for (int k = 0; k < o.ncells; k++)
                 m |= 1ull << (o.cr[k] * (int)width + o.cc[k] + x);
-            out.plc.push_back(Plc{ m, o.type, 0u });
+            Plc pl{};
+            pl.mask = m;
+            pl.type = (uint8_t)o.type;
+            const TypeField &tf = out.fields[o.type];
+            pl.off = (uint8_t)__builtin_ctzll(tf.fm);
+            pl.bits = (uint8_t)__builtin_popcountll(tf.fm);
+            pl.count = out.counts[o.type];
+            out.plc.push_back(pl);
             out.plc_type.push_back((uint16_t)o.type);
             out.plc_orient.push_back(o.t);
         }
@@ -241,7 +248,7 @@ std::string build_piece_lib(const uint64_t *shapes, const uint32_t *counts, uint
         for (size_t i = len; i-- > 0;) {
             Plc &p = out.plc[out.col_off[col] + i];
             const bool last = i + 1 == len || out.plc[out.col_off[col] + i + 1].type != p.type;
-            p.next_type = last ? (uint32_t)(i + 1) : out.plc[out.col_off[col] + i + 1].next_type;
+            p.next_type = last ? (uint8_t)(i + 1) : out.plc[out.col_off[col] + i + 1].next_type;
         }
     }
 

@@ -197,6 +197,12 @@ __device__ __forceinline__ void load_table(SmemTable &st, const InstDesc *__rest
     }
 }
 
+// Copy counter tests straight from a placement record.
+__device__ __forceinline__ bool plc_free(const Plc &p, unsigned long long u) {
+    return ((u >> p.off) & ((1ull << p.bits) - 1ull)) < (unsigned long long)p.count;
+}
+__device__ __forceinline__ unsigned long long plc_inc(const Plc &p) { return 1ull << p.off; }
+
 // Depth-first enumeration of the whole-row fills of one state (window w,
 // copy counters u).  The fill stack lives in two registers: 8-bit placement
 // index and 4-bit anchor column per depth (a row of <= 8 cells takes <= 8
@@ -382,6 +388,26 @@ __global__ void __launch_bounds__(kExpandBlock, 4)
 k_expand(ExpandArgs a) {
     __shared__ WarpStage stage[kWarps];
     const unsigned lane = threadIdx.x & 31u;
+    // Single-instance launch: the instance's descriptor and placement table
+    // staged in shared memory (dynamic), read there by every walk step.
+    const InstDesc *st_d = nullptr;
+    const Plc *st_plc = nullptr;
+    if (a.stage_plc) {
+        extern __shared__ __align__(16) unsigned char x_stage[];
+        const InstDesc *gd = a.insts + a.segs[0].inst;
+        const unsigned long long *src = reinterpret_cast<const unsigned long long *>(gd);
+        unsigned long long *dst = reinterpret_cast<unsigned long long *>(x_stage);
+        for (uint32_t i = threadIdx.x; i < sizeof(InstDesc) / 8; i += blockDim.x)
+            dst[i] = src[i];
+        const ulonglong2 *ps = reinterpret_cast<const ulonglong2 *>(a.plc + gd->plc_off);
+        ulonglong2 *pd = reinterpret_cast<ulonglong2 *>(x_stage + kStageDescBytes);
+        const uint32_t np = gd->n_plc;
+        for (uint32_t i = threadIdx.x; i < np; i += blockDim.x)
+            pd[i] = ps[i];
+        __syncthreads();
+        st_d = reinterpret_cast<const InstDesc *>(x_stage);
+        st_plc = reinterpret_cast<const Plc *>(x_stage + kStageDescBytes);
+    }
     WarpStage &ws = stage[threadIdx.x >> 5];
     const unsigned lt_mask = (1u << lane) - 1u;
     const uint32_t fan = a.fan ? a.fan : 1u;
@@ -454,8 +480,8 @@ k_expand(ExpandArgs a) {
             if (((need >> lane) & 1u) && rank < take) {
                 const unsigned long long item = c_next + rank;
                 sg = a.segs + c_seg;
-                d = a.insts + sg->inst;
-                plc = a.plc + d->plc_off;
+                d = st_d ? st_d : a.insts + sg->inst;
+                plc = st_plc ? st_plc : a.plc + d->plc_off;
                 W = d->width;
                 rowmask = (1u << W) - 1u;
                 dyn_bits = d->dyn_bits;
@@ -500,13 +526,12 @@ k_expand(ExpandArgs a) {
                         if (choice < d->col_len[c]) {
                             const Plc p = plc[d->col_off[c] + choice];
                             if (!(p.mask & ~w)) {
-                                const TypeField f = d->types[p.type];
-                                if ((u & f.fm) < f.cap) {
+                                if (plc_free(p, u)) {
                                     sidx |= (unsigned long long)choice << (8 * depth);
                                     scol |= c << (4 * depth);
                                     ++depth;
                                     w &= ~p.mask;
-                                    u += f.fm & (0ull - f.fm);
+                                    u += plc_inc(p);
                                     active = true;
                                     min_depth = depth;
                                 }
@@ -555,9 +580,9 @@ k_expand(ExpandArgs a) {
                     __shfl_sync(0xffffffffu, (unsigned long long)sg, src);
                 if (recv) {
                     sg = reinterpret_cast<const Seg *>(d_sg);
-                    d = a.insts + sg->inst;
+                    d = st_d ? st_d : a.insts + sg->inst;
                     wit = (d->flags & kInstWitness) != 0u;
-                    plc = a.plc + d->plc_off;
+                    plc = st_plc ? st_plc : a.plc + d->plc_off;
                     W = d->width;
                     rowmask = (1u << W) - 1u;
                     dyn_bits = d->dyn_bits;
@@ -577,8 +602,7 @@ k_expand(ExpandArgs a) {
                     // New subtree root: the old root with its choice placed.
                     const Plc p = plc[d->col_off[cc] + ci];
                     rw &= ~p.mask;
-                    const unsigned long long fm = d->types[p.type].fm;
-                    ru += fm & (0ull - fm);
+                    ru += plc_inc(p);
                     ++min_depth;
                 }
             }
@@ -629,13 +653,12 @@ k_expand(ExpandArgs a) {
                 if (found) {
                     const Plc p = plc[d->col_off[c] + idx];
                     if (!(p.mask & ~w)) {
-                        const TypeField f = d->types[p.type];
-                        if ((u & f.fm) < f.cap) {
+                        if (plc_free(p, u)) {
                             sidx |= (unsigned long long)idx << (8 * depth);
                             scol |= c << (4 * depth);
                             ++depth;
                             w &= ~p.mask;
-                            u += f.fm & (0ull - f.fm);
+                            u += plc_inc(p);
                             idx = 0;
                         } else {
                             idx = p.next_type;   // no copies left: skip the type's run
@@ -658,8 +681,7 @@ k_expand(ExpandArgs a) {
                     scol &= ~(0xFu << (4 * depth));
                     const Plc p = plc[d->col_off[c] + idx];
                     w |= p.mask;
-                    const unsigned long long fm = d->types[p.type].fm;
-                    u -= fm & (0ull - fm);
+                    u -= plc_inc(p);
                     ++idx;
                 }
             }
@@ -1349,10 +1371,11 @@ cudaError_t expand_max_blocks_per_sm(bool k64, int *n) {
 void launch_expand(bool k64, const ExpandArgs &a, int grid, cudaStream_t s) {
     if (a.n_chunks == 0)
         return;
+    const size_t dyn = a.stage_plc ? expand_stage_bytes(a.stage_plc) : 0;
     if (k64)
-        k_expand<true><<<grid, kExpandBlock, 0, s>>>(a);
+        k_expand<true><<<grid, kExpandBlock, dyn, s>>>(a);
     else
-        k_expand<false><<<grid, kExpandBlock, 0, s>>>(a);
+        k_expand<false><<<grid, kExpandBlock, dyn, s>>>(a);
 }
 
 namespace {

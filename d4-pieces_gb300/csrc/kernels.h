@@ -34,6 +34,10 @@ struct ExpandArgs {
     unsigned long long *work;        // dynamic chunk counter, zeroed before launch
     unsigned int max_probe;
     uint32_t prefetch;               // request each child's table line into L2 when staged
+    // Single-instance launches (one segment): the instance's n_plc
+    // placements (0 = not staged) and its descriptor are copied into shared
+    // memory at block start (expand_stage_bytes(stage_plc) dynamic bytes).
+    uint32_t stage_plc;
     // Partitioned dedup (K64 only): children are appended to bucket
     // hi(hash(key) * n_bkt) instead of inserted into the table; bucket b
     // holds records [b * bkt_cap, b * bkt_cap + bkt_cnt[b]).
@@ -76,6 +80,14 @@ struct CompactArgs {
     const unsigned long long *keep_max;
     unsigned int *status;            // kStatusCompactStall is or'ed in here
 };
+
+// Shared-memory bytes of a staged instance: its descriptor (rounded to 16)
+// and n_plc 16-byte placements.
+constexpr size_t kStageDescBytes = (sizeof(InstDesc) + 15) / 16 * 16;
+constexpr size_t expand_stage_bytes(uint32_t n_plc) { return kStageDescBytes + 16ull * n_plc; }
+// Largest staged instance (4 resident blocks per SM keep their ~18 KB of
+// child staging plus this, and leave most of L1 to the candidate filters).
+constexpr size_t kStageMaxBytes = 24 * 1024;
 
 // Resident k_expand blocks per SM (for sizing its persistent grid).
 cudaError_t expand_max_blocks_per_sm(bool k64, int *n);
