@@ -1149,6 +1149,7 @@ StepStats Engine::step_impl() {
 
         // This group's next segments follow the previous groups' ones.
         const uint64_t off0 = off;
+        const size_t nseg0 = nseg.size();
         for (size_t k = 0; k < grp.size(); k++) {
             const uint32_t id = grp[k];
             if (redo[k])
@@ -1174,9 +1175,42 @@ StepStats Engine::step_impl() {
                 off += u;
             }
         }
-        keys_[nxt].reserve(std::max<uint64_t>(off, 1), stream_, off0);
-        if (!k64_)
-            cnts_[nxt].reserve(std::max<uint64_t>(off, 1), stream_, off0);
+        // The next frontier must hold the group's distinct states.  When the
+        // device cannot hold them (the rows' growth outran the estimate that
+        // admitted them), the group's largest instances fail alone with
+        // D4E_ERR_NOMEM -- their children are dropped by the compaction --
+        // until the rest fit.
+        for (;;) {
+            try {
+                keys_[nxt].reserve(std::max<uint64_t>(off, 1), stream_, off0);
+                if (!k64_)
+                    cnts_[nxt].reserve(std::max<uint64_t>(off, 1), stream_, off0);
+                break;
+            } catch (const Error &e) {
+                if (e.code != kErrNoMem || !opts_.isolate_failures || nseg.size() == nseg0)
+                    throw;
+                cudaGetLastError();
+                size_t big = nseg0;
+                for (size_t q = nseg0; q < nseg.size(); q++)
+                    if (h_unique_[nseg[q].first] > h_unique_[nseg[big].first])
+                        big = q;
+                const uint32_t id = nseg[big].first;
+                const uint64_t u = h_unique_[id];
+                h_cursor_[id] = kCursorDrop;
+                fail_instance(id, kErrNoMem,
+                              "row does not fit the device: " + std::to_string(u) +
+                                  " distinct states in the next frontier");
+                st.failed++;
+                st.n_out -= u;
+                nseg.erase(nseg.begin() + (std::ptrdiff_t)big);
+                off = off0;
+                for (size_t q = nseg0; q < nseg.size(); q++) {
+                    nseg[q].second = off;
+                    h_cursor_[nseg[q].first] = off;
+                    off += h_unique_[nseg[q].first];
+                }
+            }
+        }
         cuda_check(cudaMemcpyAsync(cursor_.p, h_cursor_.data(),
                                    n_inst * sizeof(unsigned long long), cudaMemcpyHostToDevice,
                                    stream_),
