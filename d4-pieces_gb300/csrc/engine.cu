@@ -84,6 +84,13 @@ template <class T>
 void DevBuf<T>::reserve(size_t n, cudaStream_t stream, size_t keep) {
     if (n <= cap)
         return;
+    if (p && !keep) {
+        // Nothing to carry over: give the old block back first, so that the
+        // pool can hand its memory to the new one.
+        cuda_check(cudaFreeAsync(p, s), "cudaFreeAsync");
+        p = nullptr;
+        cap = 0;
+    }
     size_t nc = std::max(n, cap + cap / 2);
     T *np = nullptr;
     if (engine_malloc_async(reinterpret_cast<void **>(&np), nc * sizeof(T), stream) !=
@@ -91,13 +98,31 @@ void DevBuf<T>::reserve(size_t n, cudaStream_t stream, size_t keep) {
         // Geometric growth did not fit: take exactly what is needed.
         cudaGetLastError();
         nc = n;
-        cuda_check(engine_malloc_async(reinterpret_cast<void **>(&np), nc * sizeof(T), stream),
-                   "cudaMallocAsync");
+        if (engine_malloc_async(reinterpret_cast<void **>(&np), nc * sizeof(T), stream) !=
+            cudaSuccess) {
+            // The pools' free blocks may be too scattered for one large
+            // block: once the stream's frees have happened, return every
+            // unused block to the driver (this engine's pool and the idle
+            // ones) and try once more.
+            cudaGetLastError();
+            cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+            cudaMemPool_t pool = nullptr;
+            if (tl_pool_ref && *tl_pool_ref)
+                pool = *tl_pool_ref;
+            else {
+                int dev = 0;
+                cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+                cuda_check(cudaDeviceGetDefaultMemPool(&pool, dev), "cudaDeviceGetDefaultMemPool");
+            }
+            cuda_check(cudaMemPoolTrimTo(pool, 0), "cudaMemPoolTrimTo");
+            release_idle_pools();
+            cuda_check(engine_malloc_async(reinterpret_cast<void **>(&np), nc * sizeof(T), stream),
+                       ("cudaMallocAsync of " + std::to_string(nc * sizeof(T)) + " bytes").c_str());
+        }
     }
     if (p) {
-        if (keep)
-            cuda_check(cudaMemcpyAsync(np, p, keep * sizeof(T), cudaMemcpyDeviceToDevice, stream),
-                       "cudaMemcpyAsync");
+        cuda_check(cudaMemcpyAsync(np, p, keep * sizeof(T), cudaMemcpyDeviceToDevice, stream),
+                   "cudaMemcpyAsync");
         cuda_check(cudaFreeAsync(p, s), "cudaFreeAsync");
     }
     p = np;

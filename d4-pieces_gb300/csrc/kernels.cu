@@ -4,15 +4,17 @@
 //   k_expand  : replaces the reference's tiled_row_search / linear_row_search
 //               + impl<H> (src/kernel.cuh:12-227).  Each state is expanded by
 //               every whole-row fill -- a depth-first walk over placements
-//               anchored at the lowest empty cell of the current row, with
-//               the instance's placement table and candidate filters read
-//               through L1 -- and
-//               each child is inserted straight into an HBM-resident
+//               anchored at the lowest empty cell of the current row.  A
+//               single-instance launch first stages the instance's placement
+//               table and descriptor in shared memory; the candidate filters
+//               (and, in batches, every table) are read through L1.  Each
+//               child is inserted straight into an HBM-resident
 //               open-addressing table (key CAS + 64-bit count add), which
 //               replaces the reference's ring buffer + host hash-set Sorter
 //               (src/device.cu:14-309, src/sorter.cpp:72-214).
-//   k_compact : moves the table into the next frontier, instance by
-//               instance, clearing it for the next row.
+//   k_compact : streams the table through shared memory (1-D bulk copies)
+//               into the next frontier, instance by instance, clearing it
+//               for the next row.
 // Both are templated on the key encoding (K64 packed / K128 general, see
 // d4e_types.h).
 #include "kernels.h"
@@ -378,9 +380,11 @@ __device__ __forceinline__ uint32_t flush_children(const ExpandArgs &a, const Wa
 // thousands of row fills spreads over many lanes.  Every iteration of the
 // warp loop performs exactly one step of each lane's depth-first walk --
 // test one candidate placement, descend, backtrack, or complete the row --
-// so the lanes do uniform work.  Placement tables are read through L1 from
-// global memory; each lane keeps its own instance, so a warp may move to a
-// chunk of another instance while some lanes finish earlier items.
+// so the lanes do uniform work.  A launch over one instance reads its
+// placement table and descriptor from shared memory (staged at block start);
+// batched launches read every instance's tables through L1, and each lane
+// keeps its own instance, so a warp may move to a chunk of another instance
+// while some lanes finish earlier items.
 // Completed rows are staged in shared memory and inserted by the whole
 // warp, 32 at a time.
 template <bool K64>
