@@ -84,6 +84,7 @@ template <class T>
 void DevBuf<T>::reserve(size_t n, cudaStream_t stream, size_t keep) {
     if (n <= cap)
         return;
+    size_t nc = std::max(n, cap + cap / 2);
     if (p && !keep) {
         // Nothing to carry over: give the old block back first, so that the
         // pool can hand its memory to the new one.
@@ -91,7 +92,6 @@ void DevBuf<T>::reserve(size_t n, cudaStream_t stream, size_t keep) {
         p = nullptr;
         cap = 0;
     }
-    size_t nc = std::max(n, cap + cap / 2);
     T *np = nullptr;
     if (engine_malloc_async(reinterpret_cast<void **>(&np), nc * sizeof(T), stream) !=
         cudaSuccess) {
@@ -330,9 +330,8 @@ Engine::~Engine() {
 }
 
 void Engine::ensure_inst_capacity(size_t n) {
+    // Each buffer grows on its own (a growth may fall back to the exact size).
     const size_t old = inst_.size();
-    if (n <= insts_.cap)
-        return;
     insts_.reserve(n, stream_, old);
     inst_unique_.reserve(n, stream_, 0);
     cursor_.reserve(n, stream_, 0);
