@@ -223,9 +223,11 @@ def measured_peaks() -> dict:
 
 
 def profiled_traffic() -> dict | None:
-    """Per-launch DRAM bytes of k_expand on this workload from an ncu capture
-    (profiles/k_expand_single_large.json), when one is committed."""
-    p = REPO / "profiles" / "k_expand_single_large.json"
+    """DRAM bytes per raw child of k_expand from a one-launch ncu capture of
+    the medium case (profiles/k_expand_medium_dram.json), when committed:
+    every child is an insert into a random slot of a table far larger than
+    L2, so the traffic of a launch grows with its raw children."""
+    p = REPO / "profiles" / "k_expand_medium_dram.json"
     if p.exists():
         return json.loads(p.read_text())
     return None
@@ -400,8 +402,9 @@ def bench_ours(args, dist: Dist) -> None:
     achieved = alg_bytes / (exp_ms / 1e3) / 1e9 if exp_ms > 0 else None
     traffic = profiled_traffic()
     traffic_per_launch = None
-    if traffic and traffic.get("workload") == workload:
-        traffic_per_launch = traffic.get("dram_bytes_per_launch")
+    if traffic and exp_launches:
+        traffic_per_launch = (traffic["dram_bytes_per_raw_child"] *
+                              sum(s["states_raw"] for s in st) / exp_launches)
     # Dedup output stage (k_compact): scans every table slot, writes each
     # distinct state once and clears its slot.
     cmp_ms = sum(s["compact_ms"] for s in st)
@@ -466,6 +469,8 @@ def bench_ours(args, dist: Dist) -> None:
             "traffic": traffic_per_launch,
             "algorithmic_bytes_per_launch": alg_bytes / exp_launches if exp_launches else None,
             "algorithmic_bytes": "24 B x (parent states read + raw children inserted) per launch",
+            "traffic_source": ("ncu DRAM bytes per raw child of one medium-case launch "
+                               "(profiles/k_expand_medium_dram.md) x raw children per launch"),
             "avg_launch_ms": exp_ms / exp_launches if exp_launches else None,
             "launches": exp_launches,
         },
