@@ -446,7 +446,9 @@ def bench_ours(args, dist: Dist) -> None:
                             "chunk_cap": st[0]["tuned_chunk_cap"],
                             "chunks_per_warp": st[0]["tuned_chunks_per_warp"],
                             "ctas_per_sm": st[0]["tuned_ctas_per_sm"] or "occupancy",
-                            "table_load": st[0]["tuned_load"]},
+                            "table_load": st[0]["tuned_load"],
+                            "compact_ctas_per_sm": st[0]["tuned_compact_ctas"],
+                            "compact_stages": st[0]["tuned_compact_stages"]},
             "slot_bytes": st[0]["slot_bytes"],
             "l2": "frontier and table far larger than L2 (GBs); plus a 512 MiB L2 flush between steps",
             "parallelism": f"replicas x{dist.world} (no sharding, no collectives)",

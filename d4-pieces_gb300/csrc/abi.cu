@@ -359,6 +359,8 @@ static void fill_stats(const d4e::Engine &e, d4e_stats *st, bool add = false) {
     st->tuned_chunks_per_warp = tu.chunks_per_warp;
     st->tuned_ctas_per_sm = (uint64_t)std::max(tu.ctas_per_sm, 0);
     st->tuned_load = tu.load;
+    st->tuned_compact_ctas = (uint64_t)tu.compact_ctas;
+    st->tuned_compact_stages = tu.compact_stages;
     st->compact_slots += t.compact_slots;
     const double ph[6] = {t.ph_select_ms, t.ph_table_ms, t.ph_expand_ms, t.ph_post_ms,
                           t.ph_compact_ms, t.ph_tail_ms};

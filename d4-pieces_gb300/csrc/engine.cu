@@ -1275,7 +1275,8 @@ StepStats Engine::step_impl() {
         c.inst_mask = inst_mask_;
         c.keep_max = sampled.empty() ? nullptr : keep_max_.p;
         c.status = misc_.p;
-        const int cgrid = compact_grid(ccap, sms_);
+        c.stages = tune_.compact_stages;
+        const int cgrid = compact_grid(ccap, sms_, tune_.compact_ctas);
         phase(tot_.ph_post_ms);
         cuda_check(cudaEventRecord(ev_[2], stream_), "cudaEventRecord");
         launch_compact(k64_, c, cgrid, stream_);
@@ -1585,6 +1586,7 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
                                cudaMemcpyHostToDevice, stream_),
                "upload cursors");
     (void)est;
+    double last_compact_ms = 0;   // k_compact part of the last trial
     auto trial = [&](const Tuning &t) -> double {
         const uint64_t cap = plan(t);
         if (!cap)
@@ -1637,9 +1639,11 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
         c.inst_mask = inst_mask_;
         c.keep_max = nullptr;
         c.status = misc_.p;
-        const int cgrid = compact_grid(cap, sms_);
+        c.stages = t.compact_stages;
+        const int cgrid = compact_grid(cap, sms_, t.compact_ctas);
         cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
         launch_expand(k64_, a, grid, stream_);
+        cuda_check(cudaEventRecord(ev_[2], stream_), "cudaEventRecord");
         launch_compact(k64_, c, cgrid, stream_);
         cuda_check(cudaGetLastError(), "autotune launch");
         cuda_check(cudaEventRecord(ev_[1], stream_), "cudaEventRecord");
@@ -1648,8 +1652,10 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
                    "read status");
         cuda_check(cudaStreamSynchronize(stream_), "autotune trial");
         tot_.other_launches += 2;
-        float ms = 0.f;
+        float ms = 0.f, cms = 0.f;
         cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
+        cudaEventElapsedTime(&cms, ev_[2], ev_[1]);
+        last_compact_ms = cms;
         for (uint32_t id : grp)
             inst_[id].min_region = 0;
         if (stt & kStatusCompactStall)
@@ -1689,6 +1695,26 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
         Tuning t = base3;
         t.load = load;
         consider(t);
+    }
+    // The dedup tile plan (k_compact blocks per SM x ring depth), judged on
+    // the compaction's own time, a few percent of the trial's.
+    {
+        trial(best);
+        double best_cms = last_compact_ms;
+        const Tuning base4 = best;
+        for (const auto &[ctas, stages] : {std::pair<int, uint32_t>{2, 2},
+                                           std::pair<int, uint32_t>{1, 6}}) {
+            if (!compact_plan_ok(ctas, stages))
+                continue;
+            Tuning t = base4;
+            t.compact_ctas = ctas;
+            t.compact_stages = stages;
+            if (trial(t) < 1e29 && last_compact_ms < best_cms * kTuneGain) {
+                best_cms = last_compact_ms;
+                best.compact_ctas = ctas;
+                best.compact_stages = stages;
+            }
+        }
     }
     best.set = true;
     tune_ = best;

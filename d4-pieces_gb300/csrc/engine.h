@@ -125,6 +125,8 @@ struct Tuning {
     uint32_t chunks_per_warp = 8;    // chunks per resident warp aimed at
     int ctas_per_sm = 0;             // k_expand CTAs per SM (0 = occupancy)
     double load = 0.5;               // hash table load factor aimed at
+    int compact_ctas = 2;            // k_compact blocks per SM
+    uint32_t compact_stages = 3;     // k_compact shared-memory ring depth (32 KB tiles)
 };
 
 // Count: tilings.  SolveOne: one tiling.  Sets: the piece multisets that

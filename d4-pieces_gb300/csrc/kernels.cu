@@ -751,8 +751,9 @@ k_expand(ExpandArgs a) {
 // Compaction streams the table in tiles of kCompactTileBytes (2048 K64 or
 // 1024 K128 slots; slot tile_base + j * kCompactBlock + thread for round j).
 // The tiles come into shared memory by 1-D bulk copies (cp.async.bulk, the
-// async copy engine), kCompactStages deep per block, so every block keeps
-// ~64 KB of the table in flight while it works on the tile it holds.  When
+// async copy engine), CompactArgs::stages deep per block (3 by default, two
+// blocks per SM: ~64 KB of the table in flight per block while it works on
+// the tile it holds; the launch plan can trade blocks for stages).  When
 // every occupied slot of a tile belongs to one instance -- always for a
 // single puzzle, and for every tile of a batch, whose instances own whole
 // tiles -- the block computes output positions with ballots and one shared
@@ -761,9 +762,8 @@ k_expand(ExpandArgs a) {
 // with __match_any_sync aggregation instead.  Occupied slots are cleared in
 // the table as they are taken.
 constexpr int kCompactTileBytes = 32768;
-constexpr int kCompactStages = 3;
+constexpr int kCompactMaxStages = 6;
 constexpr int kCompactWarps = kCompactBlock / 32;
-constexpr int kCompactSmem = kCompactTileBytes * kCompactStages;
 // A staged tile that has not arrived after this long (never expected: the
 // copy engine reads device memory the kernel owns) ends the launch with
 // kStatusCompactStall instead of waiting on.
@@ -1040,7 +1040,8 @@ k_compact(CompactArgs a) {
     constexpr uint32_t kSlotBytes = K64 ? 16u : 32u;
     constexpr unsigned long long kTile = (unsigned long long)PER * kCompactBlock;   // slots
     extern __shared__ __align__(128) unsigned char c_stage[];
-    __shared__ __align__(8) unsigned long long bars[kCompactStages];
+    __shared__ __align__(8) unsigned long long bars[kCompactMaxStages];
+    const uint32_t S = a.stages;
     __shared__ CompactShared<PER> sh;
     const unsigned long long n_tiles = (a.cap + kTile - 1) / kTile;
     const unsigned long long mine =
@@ -1049,25 +1050,25 @@ k_compact(CompactArgs a) {
     auto issue = [&](unsigned long long k) {
         const unsigned long long first = (blockIdx.x + k * gridDim.x) * kTile;
         const unsigned long long n = a.cap - first < kTile ? a.cap - first : kTile;
-        unsigned long long *bar = &bars[k % kCompactStages];
+        unsigned long long *bar = &bars[k % S];
         const uint32_t bytes = (uint32_t)n * kSlotBytes;
         mbar_expect_tx(bar, bytes);
-        bulk_load(c_stage + (k % kCompactStages) * kCompactTileBytes,
+        bulk_load(c_stage + (k % S) * kCompactTileBytes,
                   static_cast<const unsigned char *>(a.table) + first * kSlotBytes, bytes, bar);
     };
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kCompactStages; s++)
+        for (uint32_t s = 0; s < S; s++)
             mbar_init(&bars[s], 1);
         fence_mbar_init();
         fence_proxy_async_smem();
-        for (unsigned long long k = 0; k < mine && k < (unsigned long long)kCompactStages; k++)
+        for (unsigned long long k = 0; k < mine && k < (unsigned long long)S; k++)
             issue(k);
     }
     __syncthreads();
     unsigned long long k = 0;
     for (; k < mine; k++) {
-        const int s = (int)(k % kCompactStages);
-        const uint32_t parity = (uint32_t)((k / kCompactStages) & 1ull);
+        const int s = (int)(k % S);
+        const uint32_t parity = (uint32_t)((k / S) & 1ull);
         const bool ok = mbar_wait_bounded(&bars[s], parity);
         if (__syncthreads_or(!ok))
             break;
@@ -1085,9 +1086,9 @@ k_compact(CompactArgs a) {
         }
         // Every thread has read the stage: refill it with tile k + S.
         __syncthreads();
-        if (threadIdx.x == 0 && k + kCompactStages < mine) {
+        if (threadIdx.x == 0 && k + S < mine) {
             fence_proxy_async_smem();
-            issue(k + kCompactStages);
+            issue(k + S);
         }
         // Clear the taken slots for the next row.
 #pragma unroll
@@ -1107,10 +1108,10 @@ k_compact(CompactArgs a) {
         // is given up.
         if (threadIdx.x == 0) {
             atomicOr(a.status, kStatusCompactStall);
-            const unsigned long long last = mine < k + kCompactStages ? mine : k + kCompactStages;
+            const unsigned long long last = mine < k + S ? mine : k + S;
             for (unsigned long long q = k; q < last; q++)
-                mbar_wait_bounded(&bars[q % kCompactStages],
-                                  (uint32_t)((q / kCompactStages) & 1ull));
+                mbar_wait_bounded(&bars[q % S],
+                                  (uint32_t)((q / S) & 1ull));
         }
         __syncthreads();
     }
@@ -1393,13 +1394,18 @@ bool compact_unstaged() {
 }
 }  // namespace
 
-int compact_grid(unsigned long long cap, int sms) {
+int compact_grid(unsigned long long cap, int sms, int per_sm) {
     // Tiles of 32 KB (2048 K64 or 1024 K128 slots; the smaller count bounds
     // the grid either way).
     const unsigned long long tiles = (cap + 1023) / 1024;
-    const unsigned long long per_sm = compact_unstaged() ? 8ull : 2ull;
+    const unsigned long long per = compact_unstaged() ? 8ull : (unsigned long long)per_sm;
     return (int)std::max<unsigned long long>(
-        1ull, std::min<unsigned long long>(tiles, (unsigned long long)sms * per_sm));
+        1ull, std::min<unsigned long long>(tiles, (unsigned long long)sms * per));
+}
+
+bool compact_plan_ok(int per_sm, uint32_t stages) {
+    return per_sm >= 1 && stages >= 2 && stages <= (uint32_t)kCompactMaxStages &&
+           (size_t)per_sm * stages * kCompactTileBytes <= 200u * 1024u;
 }
 
 void launch_compact(bool k64, const CompactArgs &a, int grid, cudaStream_t s) {
@@ -1413,14 +1419,16 @@ void launch_compact(bool k64, const CompactArgs &a, int grid, cudaStream_t s) {
         return;
     }
     // The staging ring is dynamic shared memory beyond the default 48 KB.
+    CompactArgs b = a;
+    if (b.stages < 2 || b.stages > (uint32_t)kCompactMaxStages)
+        b.stages = kCompactDefaultStages;
+    const int smem = (int)b.stages * kCompactTileBytes;
     if (k64) {
-        cudaFuncSetAttribute(k_compact<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kCompactSmem);
-        k_compact<true><<<grid, kCompactBlock, kCompactSmem, s>>>(a);
+        cudaFuncSetAttribute(k_compact<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        k_compact<true><<<grid, kCompactBlock, smem, s>>>(b);
     } else {
-        cudaFuncSetAttribute(k_compact<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kCompactSmem);
-        k_compact<false><<<grid, kCompactBlock, kCompactSmem, s>>>(a);
+        cudaFuncSetAttribute(k_compact<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        k_compact<false><<<grid, kCompactBlock, smem, s>>>(b);
     }
 }
 

@@ -79,7 +79,15 @@ struct CompactArgs {
     // (~0 = keep all).  nullptr = no sampling.
     const unsigned long long *keep_max;
     unsigned int *status;            // kStatusCompactStall is or'ed in here
+    uint32_t stages;                 // shared-memory ring depth (32 KB tiles), 2..6; 0 = default
 };
+
+// Default k_compact plan: two blocks per SM, three 32 KB stages each.
+constexpr int kCompactDefaultCtas = 2;
+constexpr uint32_t kCompactDefaultStages = 3;
+// Plans the kernel accepts (blocks per SM x stages x 32 KB within the SM's
+// shared memory).
+bool compact_plan_ok(int per_sm, uint32_t stages);
 
 // Shared-memory bytes of a staged instance: its descriptor (rounded to 16)
 // and n_plc 16-byte placements.
@@ -101,9 +109,9 @@ void launch_expand(bool k64, const ExpandArgs &a, int grid, cudaStream_t s);
 // the table.
 void launch_compact(bool k64, const CompactArgs &a, int grid, cudaStream_t s);
 
-// k_compact grid for a table of `cap` slots (32 KB tiles, two blocks per SM,
-// each streaming its tiles through a shared-memory ring).
-int compact_grid(unsigned long long cap, int sms);
+// k_compact grid for a table of `cap` slots (32 KB tiles, `per_sm` blocks
+// per SM, each streaming its tiles through a shared-memory ring).
+int compact_grid(unsigned long long cap, int sms, int per_sm = kCompactDefaultCtas);
 
 // Solution reconstruction -------------------------------------------------
 struct KeySetArgs {

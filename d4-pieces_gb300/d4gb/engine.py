@@ -84,6 +84,8 @@ class Stats(C.Structure):
         ("partitioned", C.c_uint64),
         ("partition_fallbacks", C.c_uint64),
         ("merge_ms", C.c_double),
+        ("tuned_compact_ctas", C.c_uint64),
+        ("tuned_compact_stages", C.c_uint64),
     ]
 
     def as_dict(self) -> dict:

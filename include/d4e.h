@@ -202,6 +202,8 @@ typedef struct d4e_stats {
     uint64_t partitioned;       /* row groups de-duplicated through buckets */
     uint64_t partition_fallbacks; /* ... redone with the direct table (bucket overflow) */
     double merge_ms;            /* device time of k_bucket_merge (also in compact_ms) */
+    uint64_t tuned_compact_ctas;   /* k_compact blocks per SM in the launch plan */
+    uint64_t tuned_compact_stages; /* k_compact shared-memory ring depth (32 KB tiles) */
 } d4e_stats;
 
 int d4e_searcher_stats(const d4e_searcher *s, d4e_stats *st);
