@@ -1060,7 +1060,27 @@ StepStats Engine::step_impl() {
         if (table_.cap < units) {
             table_.release();
             table_clean_ = 0;
-            table_.reserve(units, stream_);
+            try {
+                table_.reserve(units, stream_);
+            } catch (const Error &e) {
+                // The device could not give the table the memory its limit
+                // promised: split the group, or fail a lone instance.
+                if (e.code != kErrNoMem || !opts_.isolate_failures)
+                    throw;
+                cudaGetLastError();
+                if (grp.size() > 1) {
+                    const size_t half = grp.size() / 2;
+                    work.emplace_back(grp.begin() + half, grp.end());
+                    work.emplace_back(grp.begin(), grp.begin() + half);
+                    tot_.splits++;
+                } else {
+                    fail_instance(grp[0], kErrNoMem,
+                                  "row does not fit the device: a table of " +
+                                      std::to_string(units * sizeof(ulonglong2)) + " bytes");
+                    st.failed++;
+                }
+                continue;
+            }
         }
         if (table_clean_ < units) {
             cuda_check(cudaMemsetAsync(table_.p + table_clean_, 0,
