@@ -47,7 +47,9 @@ ALG_RECORD_BYTES = 24   # per-state record of the roofline's algorithmic bytes
 MIX_INSTANCES = 8192
 MIX_MAX_STATES = 0            # no per-instance row limit: every instance counted
 SERVE_SECONDS = 2.0           # 2000 req/s arrival window (4000 requests)
-SERVE_LIGHT_SECONDS = 10.0    # 60 req/s arrival window (600 requests)
+SERVE_MID_SECONDS = 10.0      # 60 req/s arrival window (600 requests)
+SERVE_LIGHT_RATE = 8.0        # a rate the plain path keeps up with (~0.5 of its capacity)
+SERVE_LIGHT_SECONDS = 20.0    # ... for 20 s (160 requests)
 SERVE_GRACE = 15.0            # seconds after the window before unfinished requests are cut
 
 
@@ -84,8 +86,10 @@ def parse_args():
                     help="default run: per-instance row limit in the batched mix sections")
     ap.add_argument("--serve-seconds", type=float, default=SERVE_SECONDS,
                     help="default run: arrival window of the 2000 req/s serving section")
-    ap.add_argument("--serve-light-seconds", type=float, default=SERVE_LIGHT_SECONDS,
+    ap.add_argument("--serve-mid-seconds", type=float, default=SERVE_MID_SECONDS,
                     help="default run: arrival window of the 60 req/s serving section")
+    ap.add_argument("--serve-light-seconds", type=float, default=SERVE_LIGHT_SECONDS,
+                    help="default run: arrival window of the light-load serving section")
     ap.add_argument("--no-mix", action="store_true",
                     help="default run: skip the batched mix and serving sections")
     ap.add_argument("--autotune", action="store_true",
@@ -515,7 +519,9 @@ def bench_ours(args, dist: Dist) -> None:
                                                 args.mix_max_states, MIX_BEAM)
         line["served"] = serve_section(E, dev, 2000.0, args.serve_seconds, args.mix_max_states,
                                        MIX_BEAM, SERVE_GRACE)
-        line["served_light"] = serve_section(E, dev, 60.0, args.serve_light_seconds,
+        line["served_60"] = serve_section(E, dev, 60.0, args.serve_mid_seconds,
+                                          args.mix_max_states, MIX_BEAM, SERVE_GRACE)
+        line["served_light"] = serve_section(E, dev, SERVE_LIGHT_RATE, args.serve_light_seconds,
                                              args.mix_max_states, MIX_BEAM, SERVE_GRACE)
     print(json.dumps(line), flush=True)
 
@@ -986,7 +992,7 @@ def serve_plain(E, dev, arr, probs, modes, max_states, beam, grace: float) -> di
     request at a time in arrival order (FIFO), each through the engine alone
     (d4e_batch_run with one instance)."""
     n = len(arr)
-    lat, results = [], {}
+    lat, results, svc = [], {}, []
     t0 = time.perf_counter()
     deadline = t0 + arr[-1] + grace
     for i in range(n):
@@ -995,9 +1001,11 @@ def serve_plain(E, dev, arr, probs, modes, max_states, beam, grace: float) -> di
             time.sleep(arr[i] - now)
         if time.perf_counter() > deadline:
             break
+        start = time.perf_counter()
         out, _ = E.batch_run([probs[i]], mode=modes[i], sequential=True, device=dev,
                              max_states=max_states, beam=beam)
         done = time.perf_counter() - t0
+        svc.append((time.perf_counter() - start) * 1e3)
         r = out[0]
         results[i] = (r["status"], r["count"], r["found"])
         if r["status"] == 0:
@@ -1006,7 +1014,9 @@ def serve_plain(E, dev, arr, probs, modes, max_states, beam, grace: float) -> di
     cut = [(elapsed - arr[i]) * 1e3 for i in range(n) if i not in results]
     return {"completed": len(lat), "unfinished": n - len(results), "elapsed_s": elapsed,
             "puzzles_per_s": len(lat) / elapsed,
-            "latency_ms": _latency_summary(lat, cut), "results": results}
+            "latency_ms": _latency_summary(lat, cut),
+            "mean_service_ms": sum(svc) / len(svc) if svc else None,
+            "results": results}
 
 
 def serve_section(E, dev: int, rate: float, seconds: float, max_states: int, beam: int,
@@ -1022,8 +1032,10 @@ def serve_section(E, dev: int, rate: float, seconds: float, max_states: int, bea
     for i in set(rs) & set(rp):
         if rs[i][0] == 0 and rp[i][0] == 0 and rs[i] != rp[i]:
             raise RuntimeError(f"request {i}: served and plain results differ")
+    load = (rate * plain["mean_service_ms"] / 1e3) if plain["mean_service_ms"] else None
     return {"rate_req_s": rate, "arrival_window_s": seconds, "requests": len(arr),
-            "grace_s": grace, "served": served, "plain": plain,
+            "grace_s": grace, "offered_load_vs_plain_capacity": load,
+            "served": served, "plain": plain,
             "speedup_vs_plain": served["puzzles_per_s"] / plain["puzzles_per_s"]
             if plain["puzzles_per_s"] else None}
 
