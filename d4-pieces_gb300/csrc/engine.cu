@@ -1349,12 +1349,33 @@ StepStats Engine::step_impl() {
     // Paused instances: their states move unchanged to the next frontier.
     std::vector<std::pair<uint32_t, uint64_t>> moved;   // (id, new begin)
     if (!paused.empty()) {
-        uint64_t need = off;
-        for (uint32_t id : paused)
-            need += inst_[id].seg_len;
-        keys_[nxt].reserve(std::max<uint64_t>(need, 1), stream_, off);
-        if (!k64_)
-            cnts_[nxt].reserve(std::max<uint64_t>(need, 1), stream_, off);
+        // Room for the carried states; when the device cannot give it, the
+        // largest waiting instances fail alone (D4E_ERR_NOMEM) until the
+        // rest fit.
+        for (;;) {
+            uint64_t need = off;
+            for (uint32_t id : paused)
+                need += inst_[id].seg_len;
+            try {
+                keys_[nxt].reserve(std::max<uint64_t>(need, 1), stream_, off);
+                if (!k64_)
+                    cnts_[nxt].reserve(std::max<uint64_t>(need, 1), stream_, off);
+                break;
+            } catch (const Error &e) {
+                if (e.code != kErrNoMem || !opts_.isolate_failures)
+                    throw;
+                cudaGetLastError();
+                auto big = std::max_element(paused.begin(), paused.end(),
+                                            [&](uint32_t a, uint32_t b) {
+                                                return inst_[a].seg_len < inst_[b].seg_len;
+                                            });
+                fail_instance(*big, kErrNoMem,
+                              "waiting row does not fit the device next to the running ones: " +
+                                  std::to_string(inst_[*big].seg_len) + " states");
+                st.failed++;
+                paused.erase(big);
+            }
+        }
         for (uint32_t id : paused) {
             const Inst &in = inst_[id];
             if (in.seg_len) {
