@@ -45,7 +45,12 @@ ALG_RECORD_BYTES = 24   # per-state record of the roofline's algorithmic bytes
 # Batched mix and serving sections of the default run (the other configs of
 # the headline metric: batched vs plain puzzles/s, served vs plain p50/p99).
 MIX_INSTANCES = 8192
-MIX_MAX_STATES = 0            # no per-instance row limit: every instance counted
+# Per-instance limit on one row's distinct states in the mix sections: the
+# whole mix without a limit needs more than 15 minutes of GPU time (its
+# largest instances have rows of 10^8-10^9 states), so the default run
+# counts every instance whose rows stay within 2^22 states and reports the
+# rest (same set in both arms) as over the limit, by board size.
+MIX_MAX_STATES = 1 << 22
 SERVE_SECONDS = 2.0           # 2000 req/s arrival window (4000 requests)
 SERVE_MID_SECONDS = 10.0      # 60 req/s arrival window (600 requests)
 SERVE_LIGHT_RATE = 8.0        # a rate the plain path keeps up with (~0.5 of its capacity)
@@ -73,10 +78,8 @@ def parse_args():
                     help="batched solve-one: first sampled-frontier width")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: arrivals per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
-    ap.add_argument("--serve-grace", type=float, default=30.0,
+    ap.add_argument("--serve-grace", type=float, default=15.0,
                     help="serve: seconds after the window to wait for results")
-    ap.add_argument("--plain-sample", type=int, default=200,
-                    help="serve: requests timed alone for the plain per-request path")
     ap.add_argument("--cpu-budget", type=float, default=15.0,
                     help="seconds of host CPU work for the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -746,99 +749,22 @@ def _percentile(v, q):
 
 
 def bench_serve(args, dist: Dist) -> None:
-    """Serving: open-loop Poisson arrivals at --rate req/s for --duration s,
-    70% solve-one / 30% solve-all, drawn from the batched-mix distribution,
-    through the two-lane continuous-batching server.  Latency = submit to
-    result.  The plain per-request path (one request at a time, FIFO) is
-    measured on a sample of the same stream and run through the same arrival
-    times."""
-    import random
-
+    """Serving alone (--rate req/s for --duration s): the server and the
+    plain per-request path under the same Poisson arrivals."""
     from d4gb import engine as E
-    from d4gb.problem import batched_instance, verify_tiling
 
-    rng = random.Random(SERVE_SEED)
-    n = int(args.rate * args.duration)
-    t, arrivals = 0.0, []
-    for _ in range(n):
-        t += rng.expovariate(args.rate)
-        arrivals.append(t)
-    probs = [batched_instance(rng, i) for i in range(n)]
-    modes = [E.MODE_SOLVE_ONE if rng.random() < 0.7 else E.MODE_COUNT for _ in range(n)]
-
-    srv = E.Server(device=dist.local_rank, max_states=args.max_states, beam=args.beam)
-    results = {}
-    t0 = time.perf_counter()
-    for i, (p, m, ta) in enumerate(zip(probs, modes, arrivals)):
-        while True:
-            now = time.perf_counter() - t0
-            if now >= ta:
-                break
-            for r in srv.poll():
-                results[r["tag"]] = r
-            time.sleep(min(ta - now, 0.0005))
-        srv.submit(p, m, i)
-    window = time.perf_counter() - t0
-    deadline = t0 + args.duration + args.serve_grace
-    while len(results) < n and time.perf_counter() < deadline:
-        for r in srv.poll():
-            results[r["tag"]] = r
-        time.sleep(0.002)
-    elapsed = time.perf_counter() - t0
-    st = srv.stats()
-    srv.close()
-    done = [r for r in results.values() if r["status"] == 0]
-    bad = sum(1 for r in done if r["found"] and
-              not verify_tiling(probs[r["tag"]], r["grid"], r["steps"]))
-    if bad:
-        raise RuntimeError(f"{bad} served solve-one tilings fail the cover check")
-    lat = [r["latency_ms"] for r in done]
-    in_window = sum(1 for r in done if r["latency_ms"] / 1e3 + arrivals[r["tag"]] <= args.duration)
-
-    # Plain path: service time of each sampled request alone (sequential
-    # batch_run), then a FIFO single-server queue over the same arrivals.
-    k = min(n, args.plain_sample)
-    svc = []
-    for i in range(k):
-        a = time.perf_counter()
-        E.batch_run([probs[i]], mode=modes[i], sequential=True, device=dist.local_rank,
-                    max_states=args.max_states, beam=args.beam)
-        svc.append(time.perf_counter() - a)
-    # The queue runs over every arrival of the window; request i takes the
-    # measured service time of sample i mod k.
-    free_at, plain_lat = 0.0, []
-    for i in range(n):
-        start = max(arrivals[i], free_at)
-        free_at = start + svc[i % k]
-        plain_lat.append((free_at - arrivals[i]) * 1e3)
-    plain_rate = k / sum(svc)
-    plain_done_in_window = sum(1 for i in range(n)
-                               if arrivals[i] + plain_lat[i] / 1e3 <= args.duration)
-
+    sec = serve_section(E, dist.local_rank, args.rate, args.duration, args.max_states,
+                        args.beam, args.serve_grace)
     if dist.rank == 0:
         print(json.dumps({
             "metric": "served puzzles/s (Poisson arrivals, 70% solve-one / 30% solve-all)",
-            "value": len(done) / elapsed,
+            "value": sec["served"]["puzzles_per_s"],
             "unit": "puzzles/s",
             "n_gpus": dist.world,
             "config": {"workload": f"serving: Poisson {args.rate:g} req/s for {args.duration:g} s, "
                                    f"batched-mix distribution, seed {SERVE_SEED}",
                        "max_states_per_row": args.max_states, "beam": args.beam},
-            "offered": n, "completed": len(done), "completed_in_window": in_window,
-            "failed": sum(1 for r in results.values() if r["status"] != 0),
-            "unfinished": n - len(results), "elapsed_s": elapsed, "submit_window_s": window,
-            "latency_ms": {"p50": _percentile(lat, 0.5), "p99": _percentile(lat, 0.99)},
-            "frontier_states_per_s": st["states_out"] / elapsed,
-            "server": st,
-            "plain": {"sample": k, "puzzles_per_s": plain_rate,
-                      "completed_in_window": plain_done_in_window,
-                      "latency_ms": {"p50": _percentile(plain_lat, 0.5),
-                                     "p99": _percentile(plain_lat, 0.99)},
-                      "how": "service time of sampled requests alone (one at a time through "
-                             "d4e_batch_run sequential), FIFO single-server queue over all "
-                             "arrivals of the window, sample times reused cyclically"},
-            "speedup_vs_plain": (len(done) / elapsed) / plain_rate,
-            "cover_checked": sum(1 for r in done if r["found"]),
+            **sec,
         }), flush=True)
 
 
@@ -885,7 +811,12 @@ def mix_section(E, dev: int, n: int, mode: int, max_states: int, beam: int) -> d
         if (a["status"], a["count"], a["found"]) != (b["status"], b["count"], b["found"]):
             raise RuntimeError("batched and plain results differ")
     failed = [i for i, r in enumerate(outs["batched"]) if r["status"] != 0]
+    by_size: dict[str, int] = {}
+    for i in failed:
+        k = f"{probs[i].width}x{probs[i].height}"
+        by_size[k] = by_size.get(k, 0) + 1
     sec = {"instances": n, "seed": BATCHED_SEED, "max_states_per_row": max_states,
+           "failed_by_board_size": dict(sorted(by_size.items(), key=lambda kv: -kv[1])),
            "batched": arms["batched"], "plain": arms["plain"],
            "speedup_vs_plain": arms["batched"]["puzzles_per_s"] / arms["plain"]["puzzles_per_s"],
            "failed": len(failed),

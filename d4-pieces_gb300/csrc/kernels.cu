@@ -31,7 +31,7 @@ namespace d4e {
 
 namespace {
 
-constexpr int kExpandBlock = 256;
+constexpr int kExpandBlock = kExpandWarps * 32;
 constexpr int kCompactBlock = 256;
 
 
@@ -421,6 +421,7 @@ k_expand(ExpandArgs a) {
     // Warp-uniform chunk cursor.
     unsigned long long c_next = 0, c_end = 0;   // items of the current chunk not yet taken
     uint32_t c_seg = 0;
+    uint32_t taken = 0;                         // chunks this warp has taken
     bool no_more = false;
 
     // Lane walk state and context.
@@ -441,6 +442,12 @@ k_expand(ExpandArgs a) {
         unsigned need = __ballot_sync(0xffffffffu, !active);
         while (need && !no_more) {
             if (c_next >= c_end) {
+                if (a.warp_chunks && taken == a.warp_chunks) {
+                    // This warp's share is done: the rest of the row goes to
+                    // blocks launched after this one retires.
+                    no_more = true;
+                    break;
+                }
                 unsigned long long ci = 0;
                 if (lane == 0)
                     ci = atomicAdd(a.work, 1ull);
@@ -449,6 +456,7 @@ k_expand(ExpandArgs a) {
                     no_more = true;
                     break;
                 }
+                ++taken;
                 // Segment holding chunk ci: last seg with chunk_base <= ci.
                 uint32_t lo = 0, hi = a.n_segs - 1;
                 while (lo < hi) {

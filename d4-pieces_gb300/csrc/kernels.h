@@ -38,6 +38,7 @@ struct ExpandArgs {
     // placements (0 = not staged) and its descriptor are copied into shared
     // memory at block start (expand_stage_bytes(stage_plc) dynamic bytes).
     uint32_t stage_plc;
+    uint32_t warp_chunks;            // chunks a warp takes at most (0 = no limit)
     // Partitioned dedup (K64 only): children are appended to bucket
     // hi(hash(key) * n_bkt) instead of inserted into the table; bucket b
     // holds records [b * bkt_cap, b * bkt_cap + bkt_cnt[b]).
@@ -96,6 +97,9 @@ constexpr size_t expand_stage_bytes(uint32_t n_plc) { return kStageDescBytes + 1
 // Largest staged instance (4 resident blocks per SM keep their ~18 KB of
 // child staging plus this, and leave most of L1 to the candidate filters).
 constexpr size_t kStageMaxBytes = 24 * 1024;
+
+// Warps per k_expand block.
+constexpr int kExpandWarps = 8;
 
 // Resident k_expand blocks per SM (for sizing its persistent grid).
 cudaError_t expand_max_blocks_per_sm(bool k64, int *n);
