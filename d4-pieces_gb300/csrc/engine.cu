@@ -932,11 +932,6 @@ StepStats Engine::step_impl() {
                        "upload segments");
             tot_.h2d_bytes += segs.size() * sizeof(Seg);
             grid = (int)std::min<uint64_t>(n_chunks, (uint64_t)sms_ * (uint64_t)ctas);
-            if (opts_.warp_chunks) {
-                // Bounded blocks: enough of them to cover every chunk.
-                const uint64_t per_block = (uint64_t)(kExpandWarps * opts_.warp_chunks);
-                grid = (int)std::max<uint64_t>(1, (n_chunks + per_block - 1) / per_block);
-            }
             return tot;
         };
         if (opts_.autotune && !tune_.set && !fan && n_grp >= kTuneMinStates &&
@@ -1119,7 +1114,6 @@ StepStats Engine::step_impl() {
         a.max_probe = opts_.max_probe;
         a.prefetch = units * sizeof(ulonglong2) <= kPrefetchTableBytes ? 1u : 0u;
         a.stage_plc = stage_plc(segs);
-        a.warp_chunks = opts_.warp_chunks;
         cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
         launch_expand(k64_, a, grid, stream_);
         cuda_check(cudaGetLastError(), "k_expand launch");
@@ -1302,9 +1296,7 @@ StepStats Engine::step_impl() {
         c.keep_max = sampled.empty() ? nullptr : keep_max_.p;
         c.status = misc_.p;
         c.stages = tune_.compact_stages;
-        const int cgrid = compact_grid(ccap, sms_,
-                                       opts_.compact_ctas_per_sm ? opts_.compact_ctas_per_sm
-                                                                 : tune_.compact_ctas);
+        const int cgrid = compact_grid(ccap, sms_, tune_.compact_ctas);
         phase(tot_.ph_post_ms);
         cuda_check(cudaEventRecord(ev_[2], stream_), "cudaEventRecord");
         launch_compact(k64_, c, cgrid, stream_);
@@ -1676,7 +1668,6 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
         a.max_probe = opts_.max_probe;
         a.prefetch = units * sizeof(ulonglong2) <= kPrefetchTableBytes ? 1u : 0u;
         a.stage_plc = stage_plc(segs);
-        a.warp_chunks = opts_.warp_chunks;
         CompactArgs c{};
         c.table = table_.p;
         c.cap = cap;

@@ -99,14 +99,6 @@ struct EngineOpts {
     // k_expand CTAs per SM (0 = as many as fit).  A lower value leaves room
     // on every SM for kernels of another engine running concurrently.
     int expand_ctas_per_sm = 0;
-    // k_expand warps take at most this many chunks each (0 = as many as
-    // there are: persistent blocks), the grid growing to cover the row.
-    // Blocks then retire every few chunks, so kernels of a higher-priority
-    // stream get SMs as they do instead of waiting for the whole launch.
-    uint32_t warp_chunks = 0;
-    // k_compact blocks per SM (0 = the launch plan's): 1 leaves registers
-    // and shared memory on every SM to another engine's kernels.
-    int compact_ctas_per_sm = 0;
     bool high_priority = false;    // create the engine's stream at the highest priority
     // Placements fixed per work item when a frontier is too small to fill
     // the GPU (1 or 2; see the launch plan).  Two levels fill the whole GPU

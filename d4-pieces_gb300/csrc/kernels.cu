@@ -421,7 +421,6 @@ k_expand(ExpandArgs a) {
     // Warp-uniform chunk cursor.
     unsigned long long c_next = 0, c_end = 0;   // items of the current chunk not yet taken
     uint32_t c_seg = 0;
-    uint32_t taken = 0;                         // chunks this warp has taken
     bool no_more = false;
 
     // Lane walk state and context.
@@ -442,12 +441,6 @@ k_expand(ExpandArgs a) {
         unsigned need = __ballot_sync(0xffffffffu, !active);
         while (need && !no_more) {
             if (c_next >= c_end) {
-                if (a.warp_chunks && taken == a.warp_chunks) {
-                    // This warp's share is done: the rest of the row goes to
-                    // blocks launched after this one retires.
-                    no_more = true;
-                    break;
-                }
                 unsigned long long ci = 0;
                 if (lane == 0)
                     ci = atomicAdd(a.work, 1ull);
@@ -456,7 +449,6 @@ k_expand(ExpandArgs a) {
                     no_more = true;
                     break;
                 }
-                ++taken;
                 // Segment holding chunk ci: last seg with chunk_base <= ci.
                 uint32_t lo = 0, hi = a.n_segs - 1;
                 while (lo < hi) {

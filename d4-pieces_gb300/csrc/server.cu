@@ -6,10 +6,8 @@
 //   fast lane -- every request starts here, with a per-row frontier limit
 //                of kFastStates; high stream priority.
 //   slow lane -- requests whose frontier outgrew the fast lane restart here
-//                from their first row; its k_expand blocks retire every few
-//                chunks (the grid covers the row) and its compaction keeps
-//                to one block per SM, so the fast lane's higher-priority
-//                blocks take SMs as soon as slow blocks retire.
+//                from their first row; its k_expand grid leaves one CTA slot
+//                per SM free, so fast-lane kernels run beside it.
 // A heavy request therefore never holds up the rows of the light ones, and
 // both lanes' launches overlap on the device.  Each lane loop admits queued
 // requests in arrival order while the projected device bytes of everything
@@ -60,9 +58,6 @@ constexpr uint32_t kServerIdBits = 14;
 // table per request).
 constexpr uint64_t kFastStates = 1ull << 17;
 
-// Chunks a slow-lane k_expand warp takes before its block retires.
-constexpr uint32_t kSlowWarpChunks = 4;
-
 struct Request {
     uint32_t width = 0, height = 0, n_pieces = 0, sym = 0, mode = 0;
     std::vector<uint8_t> rows;
@@ -91,6 +86,8 @@ public:
         const uint64_t cap = (uint64_t)((double)total_b * 0.9);
         budget_ = opts_.memory_budget ? opts_.memory_budget
                                       : std::min<uint64_t>(150ull << 30, cap);
+        int occ = 0;
+        cuda_check(expand_max_blocks_per_sm(true, &occ), "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
         for (int l = 0; l < 2; l++) {
             Lane &ln = lane_[l];
             EngineOpts eo;
@@ -99,15 +96,8 @@ public:
             eo.memory_budget = budget_;
             eo.high_priority = l == 0;
             eo.autotune = true;
-            if (l == 1) {
-                // The slow lane's blocks retire every few chunks and its
-                // compaction keeps to one block per SM, so the fast lane's
-                // (high-priority) blocks get SMs within a fraction of a
-                // millisecond instead of sharing one slot per SM with a
-                // long persistent launch.
-                eo.warp_chunks = kSlowWarpChunks;
-                eo.compact_ctas_per_sm = 1;
-            }
+            if (l == 1 && occ > 1)
+                eo.expand_ctas_per_sm = occ - 1;
             EngineOpts e64 = eo;
             e64.k64_inst_bits = kServerIdBits;
             ln.eng[0] = std::make_unique<Engine>(e64);
