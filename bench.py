@@ -915,6 +915,8 @@ def serve_served(E, dev, arr, probs, modes, max_states, beam, grace: float) -> d
             "latency_ms": _latency_summary([r["latency_ms"] for r in done], cut),
             "cover_checked": sum(1 for r in done if r["found"]),
             "moved_to_slow_lane": st["moved"], "peak_active": st["peak_active"],
+            "lanes": {k: st[k] for k in ("lane_steps", "lane_busy_ms", "lane_kernel_ms",
+                                         "lane_inst_rows", "lane_admit_ms", "lane_collect_ms")},
             "results": {r["tag"]: (r["status"], r["count"], r["found"]) for r in results.values()}}
 
 
