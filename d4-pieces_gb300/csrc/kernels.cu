@@ -658,12 +658,28 @@ k_expand(ExpandArgs a) {
                     const Plc p = plc[d->col_off[c] + idx];
                     if (!(p.mask & ~w)) {
                         if (plc_free(p, u)) {
-                            sidx |= (unsigned long long)idx << (8 * depth);
-                            scol |= c << (4 * depth);
-                            ++depth;
-                            w &= ~p.mask;
-                            u += plc_inc(p);
-                            idx = 0;
+                            const unsigned long long nw = w & ~p.mask;
+                            if (a.early_emit && ((uint32_t)nw & rowmask) == 0u) {
+                                // The placement completes the row: the child
+                                // is emitted here and the walk stays at this
+                                // node (no descend / emit-and-pop iterations).
+                                emit = true;
+                                const unsigned long long nu = u + plc_inc(p);
+                                if constexpr (K64) {
+                                    ck0 = ((nw >> W) & dynmask) | (nu << dyn_bits) | sg->tag;
+                                } else {
+                                    ck0 = (nw >> W) | sg->in_shift;
+                                    ck1 = nu | sg->tag;
+                                }
+                                ++idx;
+                            } else {
+                                sidx |= (unsigned long long)idx << (8 * depth);
+                                scol |= c << (4 * depth);
+                                ++depth;
+                                w = nw;
+                                u += plc_inc(p);
+                                idx = 0;
+                            }
                         } else {
                             idx = p.next_type;   // no copies left: skip the type's run
                         }
