@@ -711,7 +711,8 @@ k_expand(ExpandArgs a) {
         if (emit) {
             const int pos = nbuf + __popc(em & lt_mask);
             ws.k0[pos] = ck0;
-            ws.k1[pos] = ck1;
+            if constexpr (!K64)
+                ws.k1[pos] = ck1;
             ws.cnt[pos] = cnt;
             ws.seg[pos] = (uint32_t)(sg - a.segs) | (wit ? 0x80000000u : 0u);
             // The child's home slot; for moderate tables its line is also
