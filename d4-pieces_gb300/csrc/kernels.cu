@@ -379,8 +379,9 @@ __device__ __forceinline__ uint32_t flush_children(const ExpandArgs &a, const Wa
 // placement fixed (the state's walk split `fan` ways), so a state with
 // thousands of row fills spreads over many lanes.  Every iteration of the
 // warp loop performs exactly one step of each lane's depth-first walk --
-// test one candidate placement, descend, backtrack, or complete the row --
-// so the lanes do uniform work.  A launch over one instance reads its
+// test one candidate placement and descend, or backtrack; a placement that
+// completes the row emits its child in the same step and the walk stays at
+// its node -- so the lanes do uniform work.  A launch over one instance reads its
 // placement table and descriptor from shared memory (staged at block start);
 // batched launches read every instance's tables through L1, and each lane
 // keeps its own instance, so a warp may move to a chunk of another instance
@@ -659,7 +660,7 @@ k_expand(ExpandArgs a) {
                     if (!(p.mask & ~w)) {
                         if (plc_free(p, u)) {
                             const unsigned long long nw = w & ~p.mask;
-                            if (a.early_emit && ((uint32_t)nw & rowmask) == 0u) {
+                            if (((uint32_t)nw & rowmask) == 0u) {
                                 // The placement completes the row: the child
                                 // is emitted here and the walk stays at this
                                 // node (no descend / emit-and-pop iterations).
