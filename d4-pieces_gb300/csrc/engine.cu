@@ -619,15 +619,6 @@ uint64_t Engine::table_limit() {
     return std::max<uint64_t>(limit / kRegionAlign * kRegionAlign, kRegionAlign);
 }
 
-// D4E_POP_EARLY=0: back up one step after a node's last candidate (A/B).
-static bool pop_early_enabled() {
-    static const bool on = [] {
-        const char *v = std::getenv("D4E_POP_EARLY");
-        return !(v && std::strcmp(v, "0") == 0);
-    }();
-    return on;
-}
-
 // Placements to stage in shared memory for a launch over `segs`: the
 // instance's whole table when the launch holds one instance and it fits
 // (D4E_STAGE_PLC=0 reads it through L1 instead).
@@ -1123,7 +1114,6 @@ StepStats Engine::step_impl() {
         a.max_probe = opts_.max_probe;
         a.prefetch = units * sizeof(ulonglong2) <= kPrefetchTableBytes ? 1u : 0u;
         a.stage_plc = stage_plc(segs);
-        a.pop_early = pop_early_enabled() ? 1u : 0u;
         cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
         launch_expand(k64_, a, grid, stream_);
         cuda_check(cudaGetLastError(), "k_expand launch");
@@ -1678,7 +1668,6 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
         a.max_probe = opts_.max_probe;
         a.prefetch = units * sizeof(ulonglong2) <= kPrefetchTableBytes ? 1u : 0u;
         a.stage_plc = stage_plc(segs);
-        a.pop_early = pop_early_enabled() ? 1u : 0u;
         CompactArgs c{};
         c.table = table_.p;
         c.cap = cap;

@@ -645,8 +645,6 @@ k_expand(ExpandArgs a) {
                     fb + (unsigned long long)(W * n0 + (W << W) + (c << W) +
                                               ((uint32_t)(w >> (2 * W)) & rowmask)) * fw;
                 bool found = false;
-                unsigned long long fm = 0;   // the found candidate's filter word
-                uint32_t fk = 0;             // ... and its index
                 for (uint32_t k = idx >> 6; k < fw; ++k) {
                     unsigned long long m = __ldg(f0 + k) & __ldg(f1 + k) & __ldg(f2 + k);
                     if (k == (idx >> 6))
@@ -654,12 +652,9 @@ k_expand(ExpandArgs a) {
                     if (m) {
                         idx = k * 64 + (uint32_t)(__ffsll((long long)m) - 1);
                         found = true;
-                        fm = m;
-                        fk = k;
                         break;
                     }
                 }
-                bool stay = found;   // still at this node after the step
                 if (found) {
                     const Plc p = plc[d->col_off[c] + idx];
                     if (!(p.mask & ~w)) {
@@ -685,7 +680,6 @@ k_expand(ExpandArgs a) {
                                 w = nw;
                                 u += plc_inc(p);
                                 idx = 0;
-                                stay = false;
                             }
                         } else {
                             idx = p.next_type;   // no copies left: skip the type's run
@@ -695,14 +689,6 @@ k_expand(ExpandArgs a) {
                     }
                 } else {
                     pop = true;
-                }
-                if (stay && a.pop_early) {
-                    // That was the node's last candidate (none left in the
-                    // last filter word): back up in this same step.
-                    const uint32_t kk = idx >> 6;
-                    if (kk >= fw ||
-                        (kk == fk && fk + 1 == fw && !(fm & (~0ull << (idx & 63u)))))
-                        pop = true;
                 }
             }
             if (pop) {
