@@ -31,7 +31,7 @@ constexpr size_t kNoAllocScratchBytes = (size_t)D4E_NOALLOC_SCRATCH_BYTES;
 
 // The scratch array.  In host code its name is only a host-side stand-in:
 // kernels get the device address resolved by cudaGetSymbolAddress below.
-__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
