@@ -117,6 +117,8 @@ public:
         }
         if (const char *v = std::getenv("D4E_SLOW_YIELD_MS"))
             slow_yield_ms_ = std::atof(v);
+        if (const char *v = std::getenv("D4E_FAST_STATES"))
+            fast_states_ = std::max<uint64_t>(1, std::strtoull(v, nullptr, 10));
         for (int l = 0; l < 2; l++)
             lane_[l].worker = std::thread([this, l] { loop(l); });
     }
@@ -212,7 +214,7 @@ private:
     double initial_projection(int l, const Request &r) const {
         const double per_state = 16.0 + 16.0 / 0.5;   // record + table slot at load 0.5
         const double floor_b = 1.0 * 1024 * 1024;
-        double p = l == 0 ? (double)kFastStates * per_state : lane_[l].avg_peak;
+        double p = l == 0 ? (double)fast_states_ * per_state : lane_[l].avg_peak;
         if (r.mode == D4E_MODE_SOLVE_ONE && opts_.beam)
             p = std::min(p, (double)opts_.beam * 64.0 * per_state);
         return std::max(floor_b, p);
@@ -221,7 +223,7 @@ private:
     uint64_t lane_limit(int l) const {
         if (l == 1)
             return opts_.max_states;
-        return opts_.max_states ? std::min(opts_.max_states, kFastStates) : kFastStates;
+        return opts_.max_states ? std::min(opts_.max_states, fast_states_) : fast_states_;
     }
 
     void loop(int l) {
@@ -408,7 +410,7 @@ private:
             // restart in the slow lane.
             if (l == 0 && eng.status(id) == kErrUnsupported &&
                 eng.error(id).rfind("frontier limit exceeded", 0) == 0 &&
-                (opts_.max_states == 0 || opts_.max_states > kFastStates)) {
+                (opts_.max_states == 0 || opts_.max_states > fast_states_)) {
                 r.moved = true;
                 moved.push_back(std::move(r));
             } else {
@@ -453,6 +455,7 @@ private:
     std::condition_variable done_cv_;
     std::condition_variable yield_cv_;   // fast lane stepped (slow lane may go)
     double slow_yield_ms_ = kSlowYieldMs;
+    uint64_t fast_states_ = kFastStates;   // fast-lane row limit (D4E_FAST_STATES overrides)
     std::deque<d4e_result> results_;
     d4e_server_stats st_{};
     bool stop_ = false;
