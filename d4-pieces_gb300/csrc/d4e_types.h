@@ -87,18 +87,6 @@ struct InstDesc {
     uint32_t f0_off[kMaxWidth];
     uint32_t f1_off[kMaxWidth];
     uint32_t f2_off[kMaxWidth];   // row-2 filter of column c, pattern = window row 2
-    // Used-up types (removed from the candidates before one is taken).
-    // With x = used ^ x_cap, a type's counter field is full (every copy
-    // placed) iff its field of x is zero, and
-    // z = x_h & ~((((x & x_m) + x_m) | x) & x_h) has the top bit of every full
-    // field set.  For column c, nibble j of z (bits 4j..4j+3) and value v != 0,
-    // the placements of the types whose top bits v holds:
-    //   filt_off + xt_off + ((c * n_nib + j) * 16 + v) * fwords.
-    unsigned long long x_cap;     // every type's capacity (count << offset)
-    unsigned long long x_m;       // bits of every field but its top bit
-    unsigned long long x_h;       // top bit of every field
-    uint32_t xt_off;
-    uint32_t n_nib;               // ceil(used_bits / 4)
     TypeField types[kMaxTypes];
     uint8_t rows[kMaxHeight];      // board rows, bit c = cell to cover
 };

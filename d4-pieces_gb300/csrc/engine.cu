@@ -388,11 +388,6 @@ uint32_t Engine::add(const InstanceSpec &sp) {
         d.f1_off[c] = in.lib.f1_off[c];
         d.f2_off[c] = in.lib.f2_off[c];
     }
-    d.x_cap = in.lib.x_cap;
-    d.x_m = in.lib.x_m;
-    d.x_h = in.lib.x_h;
-    d.xt_off = in.lib.xt_off;
-    d.n_nib = in.lib.n_nib;
     filt_total_ += in.lib.filters.size();
     d.n_types = (uint32_t)in.lib.fields.size();
     d.dyn_bits = in.lib.dyn_bits;
@@ -622,14 +617,6 @@ uint64_t Engine::table_limit() {
     const uint64_t limit =
         avail > 0 ? (uint64_t)(avail / ((double)slot_bytes + tune_.load * rec_bytes)) : 0;
     return std::max<uint64_t>(limit / kRegionAlign * kRegionAlign, kRegionAlign);
-}
-
-static bool drop_full_enabled() {
-    static const bool on = [] {
-        const char *v = std::getenv("D4E_DROP_FULL");
-        return !(v && std::strcmp(v, "0") == 0);
-    }();
-    return on;
 }
 
 // Placements to stage in shared memory for a launch over `segs`: the
@@ -1127,7 +1114,6 @@ StepStats Engine::step_impl() {
         a.max_probe = opts_.max_probe;
         a.prefetch = units * sizeof(ulonglong2) <= kPrefetchTableBytes ? 1u : 0u;
         a.stage_plc = stage_plc(segs);
-        a.drop_full = drop_full_enabled() ? 1u : 0u;
         cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
         launch_expand(k64_, a, grid, stream_);
         cuda_check(cudaGetLastError(), "k_expand launch");
@@ -1682,7 +1668,6 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
         a.max_probe = opts_.max_probe;
         a.prefetch = units * sizeof(ulonglong2) <= kPrefetchTableBytes ? 1u : 0u;
         a.stage_plc = stage_plc(segs);
-        a.drop_full = drop_full_enabled() ? 1u : 0u;
         CompactArgs c{};
         c.table = table_.p;
         c.cap = cap;

@@ -293,36 +293,6 @@ std::string build_piece_lib(const uint64_t *shapes, const uint32_t *counts, uint
                 }
         }
     }
-
-    // Used-up type masks: the counter fields' capacities, non-top bits and
-    // top bits, and per column, per nibble j of the top-bit vector and per
-    // nibble value v, the placements of the types whose top bits v holds.
-    std::vector<int> top_type(64, -1);
-    for (uint32_t t = 0; t < out.fields.size(); t++) {
-        const TypeField &f = out.fields[t];
-        if (!f.fm)
-            continue;
-        const int top = 63 - __builtin_clzll(f.fm);
-        out.x_cap |= f.cap;
-        out.x_h |= 1ull << top;
-        out.x_m |= f.fm & ~(1ull << top);
-        top_type[top] = (int)t;
-    }
-    out.n_nib = (out.used_bits + 3) / 4;
-    out.xt_off = (uint32_t)out.filters.size();
-    out.filters.resize(out.filters.size() + (size_t)width * out.n_nib * 16 * FW, 0ull);
-    for (uint32_t col = 0; col < width; col++)
-        for (uint32_t j = 0; j < out.n_nib; j++)
-            for (uint32_t v = 1; v < 16; v++) {
-                uint64_t *dst =
-                    &out.filters[out.xt_off + ((size_t)(col * out.n_nib + j) * 16 + v) * FW];
-                for (uint32_t i = 0; i < out.col_len[col]; i++) {
-                    const uint32_t t = out.plc[out.col_off[col] + i].type;
-                    for (uint32_t b = 0; b < 4; b++)
-                        if (((v >> b) & 1u) && top_type[4 * j + b] == (int)t)
-                            dst[i / 64] |= 1ull << (i % 64);
-                }
-            }
     return {};
 }
 

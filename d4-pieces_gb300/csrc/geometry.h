@@ -51,10 +51,6 @@ struct PieceLib {
     uint32_t f1_off[kMaxWidth] = {};
     uint32_t f2_off[kMaxWidth] = {};
     std::vector<uint64_t> filters;
-    // Used-up type masks (see InstDesc::x_cap .. n_nib), appended to
-    // `filters` at xt_off.
-    uint64_t x_cap = 0, x_m = 0, x_h = 0;
-    uint32_t xt_off = 0, n_nib = 0;
 };
 
 // Builds the tables; returns an empty string on success, else the reason.

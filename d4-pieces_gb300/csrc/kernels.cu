@@ -644,26 +644,11 @@ k_expand(ExpandArgs a) {
                 const unsigned long long *f2 =
                     fb + (unsigned long long)(W * n0 + (W << W) + (c << W) +
                                               ((uint32_t)(w >> (2 * W)) & rowmask)) * fw;
-                // Types with every copy placed: the top bit of each full
-                // copy-counter field (see InstDesc::x_cap).
-                const unsigned long long x = u ^ d->x_cap;
-                const unsigned long long z =
-                    d->x_h & ~((((x & d->x_m) + d->x_m) | x) & d->x_h);
-                const unsigned long long *xt =
-                    fb + d->xt_off + (unsigned long long)c * d->n_nib * 16u * fw;
                 bool found = false;
                 for (uint32_t k = idx >> 6; k < fw; ++k) {
                     unsigned long long m = __ldg(f0 + k) & __ldg(f1 + k) & __ldg(f2 + k);
                     if (k == (idx >> 6))
                         m &= ~0ull << (idx & 63u);
-                    // Drop the used-up types' placements, one lookup per
-                    // nibble of z holding a full field's top bit.
-                    for (unsigned long long zz = (m && a.drop_full) ? z : 0ull; zz;) {
-                        const uint32_t j = (uint32_t)(__ffsll((long long)zz) - 1) >> 2;
-                        const uint32_t v = (uint32_t)(zz >> (4u * j)) & 15u;
-                        m &= ~__ldg(xt + ((unsigned long long)j * 16u + v) * fw + k);
-                        zz &= ~(15ull << (4u * j));
-                    }
                     if (m) {
                         idx = k * 64 + (uint32_t)(__ffsll((long long)m) - 1);
                         found = true;

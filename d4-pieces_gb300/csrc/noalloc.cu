@@ -55,14 +55,12 @@ size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // Largest candidate-filter block of one instance (the fixed layout of
 // build_piece_lib): W * 2^(W-1) row-0 bitsets plus 2 * W * 2^W row-1 and
-// row-2 bitsets, then W * ceil(40 / 4) * 16 used-up type masks, each of
-// ceil(placements per column / 64) words; for W = 8 and 255 placements per
-// column that is (1024 + 4096 + 1280) * 4 = 25600 words.
+// row-2 bitsets, each of ceil(placements per column / 64) words; for W = 8
+// and 255 placements per column that is (1024 + 4096) * 4 = 20480 words.
 constexpr size_t kMaxFilterWords =
-    (((size_t)kMaxWidth << (kMaxWidth - 1)) + 2 * ((size_t)kMaxWidth << kMaxWidth) +
-     (size_t)kMaxWidth * ((kMaxUsedBits + 3) / 4) * 16) *
-    ((kMaxPlcPerCol + 63) / 64);
-static_assert(kMaxFilterWords == 25600, "filter region of the widest instance");
+    ((size_t)kMaxWidth << (kMaxWidth - 1)) * ((kMaxPlcPerCol + 63) / 64) +
+    2 * ((size_t)kMaxWidth << kMaxWidth) * ((kMaxPlcPerCol + 63) / 64);
+static_assert(kMaxFilterWords == 20480, "filter region of the widest instance");
 
 struct Layout {
     size_t desc, seg, misc, plc, filt, front[2], cnts[2], table;
@@ -146,11 +144,6 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
             d.f1_off[c] = lib.f1_off[c];
             d.f2_off[c] = lib.f2_off[c];
         }
-        d.x_cap = lib.x_cap;
-        d.x_m = lib.x_m;
-        d.x_h = lib.x_h;
-        d.xt_off = lib.xt_off;
-        d.n_nib = lib.n_nib;
         d.n_types = (uint32_t)lib.fields.size();
         d.dyn_bits = lib.dyn_bits;
         d.used_bits = lib.used_bits;
