@@ -27,12 +27,15 @@ def test_autotune_keeps_counts_and_caches(E):
     assert st["tuned_chunk_cap"] in (256, 512, 1024, 2048)
     assert st["tuned_chunks_per_warp"] in (4, 8, 16)
     assert 0.3 <= st["tuned_load"] <= 0.75
+    # The dedup tile plan: blocks per SM x shared-memory ring depth.
+    assert (st["tuned_compact_ctas"], st["tuned_compact_stages"]) in ((2, 3), (2, 2), (1, 6))
     again = E.CudaSearcher(f, rows=p.rows, autotune=True)
     again.run()
     assert again.count() == 4952290238
     st2 = again.stats()
     assert st2["tune_ms"] == 0          # plan taken from the process cache
     assert st2["tuned_chunk_cap"] == st["tuned_chunk_cap"]
+    assert st2["tuned_compact_stages"] == st["tuned_compact_stages"]
 
 
 def test_autotuned_batch_equals_plain(E):
