@@ -618,8 +618,10 @@ k_expand(ExpandArgs a) {
         unsigned long long ck0 = 0, ck1 = 0;
         if (active) {
             const uint32_t row = (uint32_t)w & rowmask;
+            bool found = false;
+            uint32_t c = 0;
             if (row == 0) {
-                // Row complete: the child, then back to the parent fill.
+                // Row complete at a work item's root: the child, then back up.
                 emit = true;
                 if constexpr (K64) {
                     ck0 = ((w >> W) & dynmask) | (u << dyn_bits) | sg->tag;
@@ -629,7 +631,7 @@ k_expand(ExpandArgs a) {
                 }
                 pop = true;
             } else {
-                const uint32_t c = __ffs(row) - 1;
+                c = __ffs(row) - 1;
                 // Next candidate >= idx whose row-0, row-1 and row-2 cells
                 // fit: AND of the column's three filter bitsets.
                 // Fixed filter layout (see build_piece_lib): offsets from
@@ -644,7 +646,6 @@ k_expand(ExpandArgs a) {
                 const unsigned long long *f2 =
                     fb + (unsigned long long)(W * n0 + (W << W) + (c << W) +
                                               ((uint32_t)(w >> (2 * W)) & rowmask)) * fw;
-                bool found = false;
                 for (uint32_t k = idx >> 6; k < fw; ++k) {
                     unsigned long long m = __ldg(f0 + k) & __ldg(f1 + k) & __ldg(f2 + k);
                     if (k == (idx >> 6))
@@ -655,54 +656,55 @@ k_expand(ExpandArgs a) {
                         break;
                     }
                 }
-                if (found) {
-                    const Plc p = plc[d->col_off[c] + idx];
-                    if (!(p.mask & ~w)) {
-                        if (plc_free(p, u)) {
-                            const unsigned long long nw = w & ~p.mask;
-                            if (((uint32_t)nw & rowmask) == 0u) {
-                                // The placement completes the row: the child
-                                // is emitted here and the walk stays at this
-                                // node (no descend / emit-and-pop iterations).
-                                emit = true;
-                                const unsigned long long nu = u + plc_inc(p);
-                                if constexpr (K64) {
-                                    ck0 = ((nw >> W) & dynmask) | (nu << dyn_bits) | sg->tag;
-                                } else {
-                                    ck0 = (nw >> W) | sg->in_shift;
-                                    ck1 = nu | sg->tag;
-                                }
-                                ++idx;
-                            } else {
-                                sidx |= (unsigned long long)idx << (8 * depth);
-                                scol |= c << (4 * depth);
-                                ++depth;
-                                w = nw;
-                                u += plc_inc(p);
-                                idx = 0;
-                            }
-                        } else {
-                            idx = p.next_type;   // no copies left: skip the type's run
-                        }
-                    } else {
-                        ++idx;
-                    }
-                } else {
-                    pop = true;
-                }
+                pop = !found;
             }
-            if (pop) {
-                if (depth == min_depth) {
-                    active = false;
-                } else {
-                    --depth;
-                    idx = (uint32_t)(sidx >> (8 * depth)) & 0xFFu;
-                    sidx &= ~(0xFFull << (8 * depth));
-                    const uint32_t c = (scol >> (4 * depth)) & 0xFu;
-                    scol &= ~(0xFu << (4 * depth));
-                    const Plc p = plc[d->col_off[c] + idx];
+            // One placement load per step: the candidate to test, or, backing
+            // up, the placement to undo (the column and index it was taken
+            // at come off the fill stack).
+            const bool up = pop && depth > min_depth;
+            if (pop && !up)
+                active = false;
+            uint32_t pc = c, pi = idx;
+            if (up) {
+                --depth;
+                pi = (uint32_t)(sidx >> (8 * depth)) & 0xFFu;
+                sidx &= ~(0xFFull << (8 * depth));
+                pc = (scol >> (4 * depth)) & 0xFu;
+                scol &= ~(0xFu << (4 * depth));
+            }
+            if (found || up) {
+                const Plc p = plc[d->col_off[pc] + pi];
+                if (up) {
                     w |= p.mask;
                     u -= plc_inc(p);
+                    idx = pi + 1;
+                } else if (!(p.mask & ~w)) {
+                    if (plc_free(p, u)) {
+                        const unsigned long long nw = w & ~p.mask;
+                        if (((uint32_t)nw & rowmask) == 0u) {
+                            // The placement completes the row: the child is
+                            // emitted here and the walk stays at this node.
+                            emit = true;
+                            const unsigned long long nu = u + plc_inc(p);
+                            if constexpr (K64) {
+                                ck0 = ((nw >> W) & dynmask) | (nu << dyn_bits) | sg->tag;
+                            } else {
+                                ck0 = (nw >> W) | sg->in_shift;
+                                ck1 = nu | sg->tag;
+                            }
+                            ++idx;
+                        } else {
+                            sidx |= (unsigned long long)idx << (8 * depth);
+                            scol |= c << (4 * depth);
+                            ++depth;
+                            w = nw;
+                            u += plc_inc(p);
+                            idx = 0;
+                        }
+                    } else {
+                        idx = p.next_type;   // no copies left: skip the type's run
+                    }
+                } else {
                     ++idx;
                 }
             }
