@@ -619,6 +619,21 @@ uint64_t Engine::table_limit() {
     return std::max<uint64_t>(limit / kRegionAlign * kRegionAlign, kRegionAlign);
 }
 
+// Whether every instance of a launch keeps its copy counters within 32 bits
+// (k_expand then works on them in 32-bit words; D4E_U32=0 never).
+bool Engine::counters_fit_u32(const std::vector<Seg> &segs) const {
+    static const bool off = [] {
+        const char *v = std::getenv("D4E_U32");
+        return v && std::strcmp(v, "0") == 0;
+    }();
+    if (off)
+        return false;
+    for (const Seg &sg : segs)
+        if (inst_[sg.inst].desc.used_bits > 32)
+            return false;
+    return true;
+}
+
 // Placements to stage in shared memory for a launch over `segs`: the
 // instance's whole table when the launch holds one instance and it fits
 // (D4E_STAGE_PLC=0 reads it through L1 instead).
@@ -1114,6 +1129,7 @@ StepStats Engine::step_impl() {
         a.max_probe = opts_.max_probe;
         a.prefetch = units * sizeof(ulonglong2) <= kPrefetchTableBytes ? 1u : 0u;
         a.stage_plc = stage_plc(segs);
+        a.u32 = counters_fit_u32(segs) ? 1u : 0u;
         cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
         launch_expand(k64_, a, grid, stream_);
         cuda_check(cudaGetLastError(), "k_expand launch");
@@ -1668,6 +1684,7 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
         a.max_probe = opts_.max_probe;
         a.prefetch = units * sizeof(ulonglong2) <= kPrefetchTableBytes ? 1u : 0u;
         a.stage_plc = stage_plc(segs);
+        a.u32 = counters_fit_u32(segs) ? 1u : 0u;
         CompactArgs c{};
         c.table = table_.p;
         c.cap = cap;

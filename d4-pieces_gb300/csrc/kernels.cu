@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <cstdlib>
 #include <cstring>
 
@@ -199,11 +200,16 @@ __device__ __forceinline__ void load_table(SmemTable &st, const InstDesc *__rest
     }
 }
 
-// Copy counter tests straight from a placement record.
-__device__ __forceinline__ bool plc_free(const Plc &p, unsigned long long u) {
-    return ((u >> p.off) & ((1ull << p.bits) - 1ull)) < (unsigned long long)p.count;
+// Copy counter tests straight from a placement record, on the counters in
+// 64-bit words or, when every counter of the launch fits 32 bits, in 32-bit
+// words (fewer instructions per walk step).
+template <class UT>
+__device__ __forceinline__ bool plc_free(const Plc &p, UT u) {
+    const UT fmask = ~(UT)0 >> (8u * sizeof(UT) - p.bits);
+    return ((u >> p.off) & fmask) < (UT)p.count;
 }
-__device__ __forceinline__ unsigned long long plc_inc(const Plc &p) { return 1ull << p.off; }
+template <class UT>
+__device__ __forceinline__ UT plc_inc(const Plc &p) { return (UT)1 << p.off; }
 
 // Depth-first enumeration of the whole-row fills of one state (window w,
 // copy counters u).  The fill stack lives in two registers: 8-bit placement
@@ -388,9 +394,10 @@ __device__ __forceinline__ uint32_t flush_children(const ExpandArgs &a, const Wa
 // while some lanes finish earlier items.
 // Completed rows are staged in shared memory and inserted by the whole
 // warp, 32 at a time.
-template <bool K64>
+template <bool K64, bool U32>
 __global__ void __launch_bounds__(kExpandBlock, 4)
 k_expand(ExpandArgs a) {
+    using UT = std::conditional_t<U32, uint32_t, unsigned long long>;
     __shared__ WarpStage stage[kWarps];
     const unsigned lane = threadIdx.x & 31u;
     // Single-instance launch: the instance's descriptor and placement table
@@ -431,10 +438,12 @@ k_expand(ExpandArgs a) {
     const Plc *plc = nullptr;
     uint32_t W = 0, rowmask = 0, dyn_bits = 0;
     unsigned long long usedmask = 0, dynmask = 0;
-    unsigned long long w = 0, u = 0, cnt = 0, sidx = 0;
+    unsigned long long w = 0, cnt = 0, sidx = 0;
+    UT u = 0;
     bool wit = false;   // solve-one instance: cnt holds the parent's witness
     uint32_t scol = 0, depth = 0, idx = 0, min_depth = 0;
-    unsigned long long rw = 0, ru = 0;   // walk state at the root of the lane's subtree
+    unsigned long long rw = 0;   // walk state at the root of the lane's subtree
+    UT ru = 0;
     int nbuf = 0;   // warp-uniform: staged children
 
     for (;;) {
@@ -497,11 +506,11 @@ k_expand(ExpandArgs a) {
                 wit = (d->flags & kInstWitness) != 0u;
                 if constexpr (K64) {
                     w = (rec.x & dynmask) | sg->hi_board;
-                    u = (rec.x >> dyn_bits) & usedmask;
+                    u = (UT)((rec.x >> dyn_bits) & usedmask);
                     cnt = wit ? witness64(rec.x, sg->tag) : rec.y;
                 } else {
                     w = rec.x;
-                    u = rec.y & kUsedMask128;
+                    u = (UT)(rec.y & kUsedMask128);
                     cnt = wit ? witness128(rec.x, rec.y) : a.cnts[si];
                 }
                 sidx = 0;
@@ -531,12 +540,12 @@ k_expand(ExpandArgs a) {
                         if (choice < d->col_len[c]) {
                             const Plc p = plc[d->col_off[c] + choice];
                             if (!(p.mask & ~w)) {
-                                if (plc_free(p, u)) {
+                                if (plc_free<UT>(p, u)) {
                                     sidx |= (unsigned long long)choice << (8 * depth);
                                     scol |= c << (4 * depth);
                                     ++depth;
                                     w &= ~p.mask;
-                                    u += plc_inc(p);
+                                    u += plc_inc<UT>(p);
                                     active = true;
                                     min_depth = depth;
                                 }
@@ -578,7 +587,7 @@ k_expand(ExpandArgs a) {
                     cc = (scol >> (4 * min_depth)) & 0xFu;
                 }
                 const unsigned long long d_rw = __shfl_sync(0xffffffffu, rw, src);
-                const unsigned long long d_ru = __shfl_sync(0xffffffffu, ru, src);
+                const UT d_ru = __shfl_sync(0xffffffffu, ru, src);
                 const unsigned long long d_cnt = __shfl_sync(0xffffffffu, cnt, src);
                 const uint32_t d_idx = __shfl_sync(0xffffffffu, ci + 1, src);
                 const unsigned long long d_sg =
@@ -607,7 +616,7 @@ k_expand(ExpandArgs a) {
                     // New subtree root: the old root with its choice placed.
                     const Plc p = plc[d->col_off[cc] + ci];
                     rw &= ~p.mask;
-                    ru += plc_inc(p);
+                    ru += plc_inc<UT>(p);
                     ++min_depth;
                 }
             }
@@ -624,10 +633,10 @@ k_expand(ExpandArgs a) {
                 // Row complete at a work item's root: the child, then back up.
                 emit = true;
                 if constexpr (K64) {
-                    ck0 = ((w >> W) & dynmask) | (u << dyn_bits) | sg->tag;
+                    ck0 = ((w >> W) & dynmask) | ((unsigned long long)u << dyn_bits) | sg->tag;
                 } else {
                     ck0 = (w >> W) | sg->in_shift;
-                    ck1 = u | sg->tag;
+                    ck1 = (unsigned long long)u | sg->tag;
                 }
                 pop = true;
             } else {
@@ -676,21 +685,21 @@ k_expand(ExpandArgs a) {
                 const Plc p = plc[d->col_off[pc] + pi];
                 if (up) {
                     w |= p.mask;
-                    u -= plc_inc(p);
+                    u -= plc_inc<UT>(p);
                     idx = pi + 1;
                 } else if (!(p.mask & ~w)) {
-                    if (plc_free(p, u)) {
+                    if (plc_free<UT>(p, u)) {
                         const unsigned long long nw = w & ~p.mask;
                         if (((uint32_t)nw & rowmask) == 0u) {
                             // The placement completes the row: the child is
                             // emitted here and the walk stays at this node.
                             emit = true;
-                            const unsigned long long nu = u + plc_inc(p);
+                            const UT nu = u + plc_inc<UT>(p);
                             if constexpr (K64) {
-                                ck0 = ((nw >> W) & dynmask) | (nu << dyn_bits) | sg->tag;
+                                ck0 = ((nw >> W) & dynmask) | ((unsigned long long)nu << dyn_bits) | sg->tag;
                             } else {
                                 ck0 = (nw >> W) | sg->in_shift;
-                                ck1 = nu | sg->tag;
+                                ck1 = (unsigned long long)nu | sg->tag;
                             }
                             ++idx;
                         } else {
@@ -698,7 +707,7 @@ k_expand(ExpandArgs a) {
                             scol |= c << (4 * depth);
                             ++depth;
                             w = nw;
-                            u += plc_inc(p);
+                            u += plc_inc<UT>(p);
                             idx = 0;
                         }
                     } else {
@@ -1389,8 +1398,8 @@ __global__ void k_count_pattern(const ulonglong2 *__restrict__ recs, unsigned lo
 }  // namespace
 
 cudaError_t expand_max_blocks_per_sm(bool k64, int *n) {
-    return k64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, k_expand<true>, kExpandBlock, 0)
-               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, k_expand<false>, kExpandBlock, 0);
+    return k64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, k_expand<true, false>, kExpandBlock, 0)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, k_expand<false, false>, kExpandBlock, 0);
 }
 
 void launch_expand(bool k64, const ExpandArgs &a, int grid, cudaStream_t s) {
@@ -1398,9 +1407,10 @@ void launch_expand(bool k64, const ExpandArgs &a, int grid, cudaStream_t s) {
         return;
     const size_t dyn = a.stage_plc ? expand_stage_bytes(a.stage_plc) : 0;
     if (k64)
-        k_expand<true><<<grid, kExpandBlock, dyn, s>>>(a);
+        a.u32 ? k_expand<true, true><<<grid, kExpandBlock, dyn, s>>>(a)
+              : k_expand<true, false><<<grid, kExpandBlock, dyn, s>>>(a);
     else
-        k_expand<false><<<grid, kExpandBlock, dyn, s>>>(a);
+        k_expand<false, false><<<grid, kExpandBlock, dyn, s>>>(a);
 }
 
 namespace {

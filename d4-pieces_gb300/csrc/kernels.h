@@ -38,6 +38,7 @@ struct ExpandArgs {
     // placements (0 = not staged) and its descriptor are copied into shared
     // memory at block start (expand_stage_bytes(stage_plc) dynamic bytes).
     uint32_t stage_plc;
+    uint32_t u32;                    // K64: every instance's copy counters fit 32 bits
     // Partitioned dedup (K64 only): children are appended to bucket
     // hi(hash(key) * n_bkt) instead of inserted into the table; bucket b
     // holds records [b * bkt_cap, b * bkt_cap + bkt_cnt[b]).
