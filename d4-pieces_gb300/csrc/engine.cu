@@ -634,6 +634,14 @@ bool Engine::counters_fit_u32(const std::vector<Seg> &segs) const {
     return true;
 }
 
+// Whether some instance of a launch has filters of more than one word.
+bool Engine::multi_word_filters(const std::vector<Seg> &segs) const {
+    for (const Seg &sg : segs)
+        if (inst_[sg.inst].desc.fwords > 1)
+            return true;
+    return false;
+}
+
 // Placements to stage in shared memory for a launch over `segs`: the
 // instance's whole table when the launch holds one instance and it fits
 // (D4E_STAGE_PLC=0 reads it through L1 instead).
@@ -1130,6 +1138,7 @@ StepStats Engine::step_impl() {
         a.prefetch = units * sizeof(ulonglong2) <= kPrefetchTableBytes ? 1u : 0u;
         a.stage_plc = stage_plc(segs);
         a.u32 = counters_fit_u32(segs) ? 1u : 0u;
+        a.single_word = multi_word_filters(segs) ? 0u : 1u;
         cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
         launch_expand(k64_, a, grid, stream_);
         cuda_check(cudaGetLastError(), "k_expand launch");
@@ -1685,6 +1694,7 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
         a.prefetch = units * sizeof(ulonglong2) <= kPrefetchTableBytes ? 1u : 0u;
         a.stage_plc = stage_plc(segs);
         a.u32 = counters_fit_u32(segs) ? 1u : 0u;
+        a.single_word = multi_word_filters(segs) ? 0u : 1u;
         CompactArgs c{};
         c.table = table_.p;
         c.cap = cap;

@@ -307,6 +307,7 @@ private:
     int expand_occupancy();
     uint32_t stage_plc(const std::vector<Seg> &segs) const;
     bool counters_fit_u32(const std::vector<Seg> &segs) const;
+    bool multi_word_filters(const std::vector<Seg> &segs) const;
     uint64_t table_limit();
     size_t slot_units() const { return k64_ ? 1 : 2; }   // table slot size in 16-byte units
     Seg seg_for(uint32_t id, uint32_t row) const;

@@ -394,7 +394,7 @@ __device__ __forceinline__ uint32_t flush_children(const ExpandArgs &a, const Wa
 // while some lanes finish earlier items.
 // Completed rows are staged in shared memory and inserted by the whole
 // warp, 32 at a time.
-template <bool K64, bool U32>
+template <bool K64, bool U32, bool MW>
 __global__ void __launch_bounds__(kExpandBlock, 4)
 k_expand(ExpandArgs a) {
     using UT = std::conditional_t<U32, uint32_t, unsigned long long>;
@@ -655,7 +655,11 @@ k_expand(ExpandArgs a) {
                 const unsigned long long *f2 =
                     fb + (unsigned long long)(W * n0 + (W << W) + (c << W) +
                                               ((uint32_t)(w >> (2 * W)) & rowmask)) * fw;
-                for (uint32_t k = idx >> 6; k < fw; ++k) {
+                // Words of this column's bitsets that can hold candidates: one
+                // when every instance of the launch has single-word filters,
+                // else as many as this column's placements need.
+                const uint32_t cfw = MW ? (((uint32_t)d->col_len[c] + 63u) >> 6) : 1u;
+                for (uint32_t k = idx >> 6; k < cfw; ++k) {
                     unsigned long long m = __ldg(f0 + k) & __ldg(f1 + k) & __ldg(f2 + k);
                     if (k == (idx >> 6))
                         m &= ~0ull << (idx & 63u);
@@ -1398,8 +1402,10 @@ __global__ void k_count_pattern(const ulonglong2 *__restrict__ recs, unsigned lo
 }  // namespace
 
 cudaError_t expand_max_blocks_per_sm(bool k64, int *n) {
-    return k64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, k_expand<true, false>, kExpandBlock, 0)
-               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, k_expand<false, false>, kExpandBlock, 0);
+    return k64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, k_expand<true, false, true>,
+                                                                kExpandBlock, 0)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, k_expand<false, false, true>,
+                                                                kExpandBlock, 0);
 }
 
 void launch_expand(bool k64, const ExpandArgs &a, int grid, cudaStream_t s) {
@@ -1407,10 +1413,15 @@ void launch_expand(bool k64, const ExpandArgs &a, int grid, cudaStream_t s) {
         return;
     const size_t dyn = a.stage_plc ? expand_stage_bytes(a.stage_plc) : 0;
     if (k64)
-        a.u32 ? k_expand<true, true><<<grid, kExpandBlock, dyn, s>>>(a)
-              : k_expand<true, false><<<grid, kExpandBlock, dyn, s>>>(a);
+        if (a.u32)
+            a.single_word ? k_expand<true, true, false><<<grid, kExpandBlock, dyn, s>>>(a)
+                          : k_expand<true, true, true><<<grid, kExpandBlock, dyn, s>>>(a);
+        else
+            a.single_word ? k_expand<true, false, false><<<grid, kExpandBlock, dyn, s>>>(a)
+                          : k_expand<true, false, true><<<grid, kExpandBlock, dyn, s>>>(a);
     else
-        k_expand<false, false><<<grid, kExpandBlock, dyn, s>>>(a);
+        a.single_word ? k_expand<false, false, false><<<grid, kExpandBlock, dyn, s>>>(a)
+                      : k_expand<false, false, true><<<grid, kExpandBlock, dyn, s>>>(a);
 }
 
 namespace {

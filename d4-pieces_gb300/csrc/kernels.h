@@ -39,6 +39,8 @@ struct ExpandArgs {
     // memory at block start (expand_stage_bytes(stage_plc) dynamic bytes).
     uint32_t stage_plc;
     uint32_t u32;                    // K64: every instance's copy counters fit 32 bits
+    uint32_t single_word;            // every instance's candidate filters are one word each
+                                     // (0, the default, is right for any launch)
     // Partitioned dedup (K64 only): children are appended to bucket
     // hi(hash(key) * n_bkt) instead of inserted into the table; bucket b
     // holds records [b * bkt_cap, b * bkt_cap + bkt_cnt[b]).
