@@ -1,8 +1,9 @@
 """The measurement switches change how the kernels work, never the results.
 
 D4E_COMPACT=ld compacts with per-thread loads instead of the shared-memory
-bulk-copy ring, and D4E_STAGE_PLC=0 reads a single puzzle's placement table
-through L1 instead of staging it in shared memory.  Each is read once per
+bulk-copy ring, D4E_STAGE_PLC=0 reads a single puzzle's placement table
+through L1 instead of staging it in shared memory, and D4E_U32=0 keeps the
+walk's copy counters in 64-bit words.  Each is read once per
 process, so each runs in a child process over golden cases (single puzzle
 and batch) whose counts must equal the reference's.
 """
@@ -38,7 +39,7 @@ print(json.dumps({"single": single, "batch": batch, "wide": wide,
 """
 
 
-@pytest.mark.parametrize("env", [{"D4E_COMPACT": "ld"}, {"D4E_STAGE_PLC": "0"}])
+@pytest.mark.parametrize("env", [{"D4E_COMPACT": "ld"}, {"D4E_STAGE_PLC": "0"}, {"D4E_U32": "0"}])
 def test_switch_keeps_counts(env):
     out = subprocess.run([sys.executable, "-c", CHILD, str(REPO)], capture_output=True,
                          text=True, timeout=600, env={**os.environ, **env})
