@@ -46,10 +46,11 @@ ALG_RECORD_BYTES = 24   # per-state record of the roofline's algorithmic bytes
 # the headline metric: batched vs plain puzzles/s, served vs plain p50/p99).
 MIX_INSTANCES = 8192
 # Per-instance limit on one row's distinct states in the mix sections: the
-# whole mix without a limit needs more than 15 minutes of GPU time (its
-# largest instances have rows of 10^8-10^9 states), so the default run
-# counts every instance whose rows stay within 2^22 states and reports the
-# rest (same set in both arms) as over the limit, by board size.
+# whole mix without a limit takes about 12 minutes of GPU time batched (its
+# largest instances have rows of 10^8-10^9 states; 95 do not fit the
+# device), so the default run counts every instance whose rows stay within
+# 2^22 states and reports the rest (same set in both arms) as over the
+# limit, by board size.
 MIX_MAX_STATES = 1 << 22
 SERVE_SECONDS = 2.0           # 2000 req/s arrival window (4000 requests)
 SERVE_MID_SECONDS = 10.0      # 60 req/s arrival window (600 requests)
