@@ -5,15 +5,20 @@ Counts are compared exactly with the reference's golden counts and the
 oracle; solve-one tilings are checked by the oracle's independent cover
 check (any valid tiling is a correct answer), and must be identical alone
 and batched."""
+import json
+
 import numpy as np
 import pytest
 
-from conftest import case_problem, load_cases
+from conftest import GOLDEN, case_problem, load_cases
 
 pytestmark = pytest.mark.gpu
 
 CASES = [c for c in load_cases() if c["width"] <= 8 and c["width"] * c["height"] <= 512]
 SMALL = [c for c in CASES if c["count"] < 10 ** 6]
+# Larger instances of the batched mix (40-71 cells), pinned by the oracle's
+# exact row DP (tests/golden/make_mix_golden.py).
+MIX_LARGE = json.loads((GOLDEN / "mix_large.json").read_text())["cases"]
 
 
 @pytest.fixture(scope="module")
@@ -26,6 +31,23 @@ def E(engine):
 def assert_valid(oracle, p, r):
     types, masks = oracle.grid_to_placements(p, r["grid"], r["steps"])
     assert oracle.check_tiling(p, types, masks), p.name
+
+
+@pytest.mark.parametrize("wide", [False, True])
+def test_batch_counts_match_oracle_on_larger_mix_instances(E, wide):
+    probs = [case_problem(c) for c in MIX_LARGE]
+    res, _ = E.batch_run(probs, wide_keys=wide)
+    assert [r["status"] for r in res] == [0] * len(probs)
+    assert [r["count"] for r in res] == [c["count"] for c in MIX_LARGE]
+
+
+def test_searcher_rows_match_oracle_on_larger_mix_instances(E):
+    for c in MIX_LARGE:
+        p = case_problem(c)
+        f = E.Frow(p.shapes, p.counts, p.sym, p.width, device=0)
+        s = E.CudaSearcher(f, rows=p.rows)
+        s.run()
+        assert (s.count(), s.level_sizes()) == (c["count"], c["level_sizes"]), c["name"]
 
 
 def test_batch_run_counts_match_reference(E):
