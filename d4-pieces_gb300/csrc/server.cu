@@ -68,6 +68,11 @@ constexpr uint64_t kFastStates = 1ull << 17;
 // req/s 293 -> 344 puzzles/s (no wait vs 10 ms).
 constexpr double kSlowYieldMs = 10.0;
 
+bool server_autotune() {
+    const char *v = std::getenv("D4E_SERVER_AUTOTUNE");
+    return v && std::strcmp(v, "1") == 0;
+}
+
 struct Request {
     uint32_t width = 0, height = 0, n_pieces = 0, sym = 0, mode = 0;
     std::vector<uint8_t> rows;
@@ -105,7 +110,10 @@ public:
             eo.isolate_failures = true;
             eo.memory_budget = budget_;
             eo.high_priority = l == 0;
-            eo.autotune = true;
+            // Launch plans are measured only when asked (D4E_SERVER_AUTOTUNE=1):
+            // the trials run inside the first large request of each board
+            // width and key encoding, which then waits for them.
+            eo.autotune = server_autotune();
             if (l == 1 && occ > 1)
                 eo.expand_ctas_per_sm = occ - 1;
             EngineOpts e64 = eo;
