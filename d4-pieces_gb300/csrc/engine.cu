@@ -263,6 +263,8 @@ Engine::Engine(const EngineOpts &opts) : opts_(opts) {
     tune_.chunk_cap = opts_.chunk_states;
     tune_.load = opts_.target_load;
     tune_.ctas_per_sm = opts_.expand_ctas_per_sm;
+    if (opts_.chunks_per_warp)
+        tune_.chunks_per_warp = opts_.chunks_per_warp;
     if (opts_.k64_inst_bits) {
         if (opts_.k64_inst_bits > 23 || opts_.keep_levels)
             throw Error(kErrInvalid, "k64_inst_bits must be 1..23 (and no keep_levels)");
@@ -1139,11 +1141,34 @@ StepStats Engine::step_impl() {
         a.stage_plc = stage_plc(segs);
         a.u32 = counters_fit_u32(segs) ? 1u : 0u;
         a.single_word = multi_word_filters(segs) ? 0u : 1u;
-        cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
-        launch_expand(k64_, a, grid, stream_);
-        cuda_check(cudaGetLastError(), "k_expand launch");
-        cuda_check(cudaEventRecord(ev_[1], stream_), "cudaEventRecord");
-        tot_.expand_launches++;
+        // A launch that honours the preemption flag may end with chunks not
+        // yet taken (the work counter below n_chunks): launch again, with
+        // the counters kept, until the row is done.
+        const bool can_preempt = opts_.preempt_flag && opts_.preempt_gate;
+        for (bool preempted = false;;) {
+            a.preempt = can_preempt && opts_.preempt_gate(preempted) ? opts_.preempt_flag
+                                                                      : nullptr;
+            cuda_check(cudaEventRecord(ev_[0], stream_), "cudaEventRecord");
+            launch_expand(k64_, a, grid, stream_);
+            cuda_check(cudaGetLastError(), "k_expand launch");
+            cuda_check(cudaEventRecord(ev_[1], stream_), "cudaEventRecord");
+            tot_.expand_launches++;
+            if (!a.preempt)
+                break;
+            unsigned long long h_taken = 0;
+            cuda_check(cudaMemcpyAsync(&h_taken, a.work, sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost, stream_),
+                       "read work counter");
+            cuda_check(cudaStreamSynchronize(stream_), "k_expand");
+            tot_.d2h_bytes += sizeof(unsigned long long);
+            if (h_taken >= n_chunks)
+                break;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
+            st.expand_ms += ms;
+            tot_.preemptions++;
+            preempted = true;
+        }
         cuda_check(cudaMemcpyAsync(&h_raw, nraw_.p, sizeof(unsigned long long),
                                    cudaMemcpyDeviceToHost, stream_),
                    "read raw");
@@ -1351,9 +1376,10 @@ StepStats Engine::step_impl() {
         if (!sampled.empty()) {
             // Kept states per sampled instance = cursor advance.
             std::vector<unsigned long long> cend(n_inst);
-            cuda_check(cudaMemcpy(cend.data(), cursor_.p, n_inst * sizeof(unsigned long long),
-                                  cudaMemcpyDeviceToHost),
+            cuda_check(cudaMemcpyAsync(cend.data(), cursor_.p, n_inst * sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost, stream_),
                        "read cursors");
+            cuda_check(cudaStreamSynchronize(stream_), "read cursors");
             tot_.d2h_bytes += n_inst * sizeof(unsigned long long);
             for (uint32_t id : sampled)
                 h_unique_[id] = (unsigned int)(cend[id] - h_cursor_[id]);
@@ -1536,17 +1562,20 @@ StepStats Engine::step_impl() {
                 // Final level: sum the counts of the stored states.
                 if (k64_) {
                     std::vector<ulonglong2> rec(in.seg_len);
-                    cuda_check(cudaMemcpy(rec.data(), lvl_keys_.back(),
-                                          in.seg_len * sizeof(ulonglong2), cudaMemcpyDeviceToHost),
+                    cuda_check(cudaMemcpyAsync(rec.data(), lvl_keys_.back(),
+                                               in.seg_len * sizeof(ulonglong2),
+                                               cudaMemcpyDeviceToHost, stream_),
                                "read final level");
+                    cuda_check(cudaStreamSynchronize(stream_), "read final level");
                     for (const auto &r : rec)
                         sum += r.y;
                 } else {
                     std::vector<unsigned long long> cn(in.seg_len);
-                    cuda_check(cudaMemcpy(cn.data(), lvl_cnts_.back(),
-                                          in.seg_len * sizeof(unsigned long long),
-                                          cudaMemcpyDeviceToHost),
+                    cuda_check(cudaMemcpyAsync(cn.data(), lvl_cnts_.back(),
+                                               in.seg_len * sizeof(unsigned long long),
+                                               cudaMemcpyDeviceToHost, stream_),
                                "read final level");
+                    cuda_check(cudaStreamSynchronize(stream_), "read final level");
                     for (auto v : cn)
                         sum += v;
                 }
@@ -2167,7 +2196,9 @@ uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t
     PathNode root{};
     {
         ulonglong2 rk;
-        cuda_check(cudaMemcpy(&rk, lvl_keys_[0], sizeof(rk), cudaMemcpyDeviceToHost), "read root");
+        cuda_check(cudaMemcpyAsync(&rk, lvl_keys_[0], sizeof(rk), cudaMemcpyDeviceToHost, stream_),
+                   "read root");
+        cuda_check(cudaStreamSynchronize(stream_), "read root");
         root.k0 = rk.x;
         root.k1 = k64_ ? 0ull : rk.y;
         root.parent = ~0u;
@@ -2194,10 +2225,12 @@ uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t
         cuda_check(cudaStreamSynchronize(stream_), "extend paths");
         const uint32_t got = std::min(hn[0], max_nodes);
         levels[r + 1].resize(got);
-        if (got)
-            cuda_check(cudaMemcpy(levels[r + 1].data(), dout.p, got * sizeof(PathNode),
-                                  cudaMemcpyDeviceToHost),
+        if (got) {
+            cuda_check(cudaMemcpyAsync(levels[r + 1].data(), dout.p, got * sizeof(PathNode),
+                                       cudaMemcpyDeviceToHost, stream_),
                        "read nodes");
+            cuda_check(cudaStreamSynchronize(stream_), "read nodes");
+        }
     }
     for (auto p : owned)
         cudaFree(p);

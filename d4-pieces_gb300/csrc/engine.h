@@ -100,6 +100,17 @@ struct EngineOpts {
     // on every SM for kernels of another engine running concurrently.
     int expand_ctas_per_sm = 0;
     bool high_priority = false;    // create the engine's stream at the highest priority
+    // Cooperative preemption of k_expand (ExpandArgs::preempt): the device
+    // address of a flag in mapped host memory, and a gate that step() calls
+    // before each k_expand launch of a row with whether the row's previous
+    // launch was preempted (false before its first).  The gate may wait; it
+    // returns whether this launch honours the flag.  A preempted launch is
+    // launched again until every chunk of the row is taken.
+    const unsigned int *preempt_flag = nullptr;
+    std::function<bool(bool)> preempt_gate;
+    // Chunks per resident warp aimed at by the launch plan (0 = the default
+    // plan).  More, smaller chunks let a preempted launch end sooner.
+    uint32_t chunks_per_warp = 0;
     // Placements fixed per work item when a frontier is too small to fill
     // the GPU (1 or 2; see the launch plan).  Two levels fill the whole GPU
     // from a handful of states, which an engine sharing the GPU with a
@@ -174,6 +185,7 @@ struct Totals {
     double expand_ms = 0.0, compact_ms = 0.0;
     uint64_t expand_launches = 0, compact_launches = 0, other_launches = 0, retries = 0;
     uint64_t paused = 0, splits = 0, failed = 0, restarts = 0;
+    uint64_t preemptions = 0;      // k_expand launches ended early by preemption
     uint64_t peak_frontier = 0;
     uint64_t h2d_bytes = 0, d2h_bytes = 0;
     double run_ms = 0.0;           // CUDA-event time from the first step to the last

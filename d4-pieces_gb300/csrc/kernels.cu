@@ -451,8 +451,8 @@ k_expand(ExpandArgs a) {
         unsigned need = __ballot_sync(0xffffffffu, !active);
         while (need && !no_more) {
             if (c_next >= c_end) {
-                unsigned long long ci = 0;
-                if (lane == 0)
+                unsigned long long ci = ~0ull;
+                if (lane == 0 && !(a.preempt && *(const volatile unsigned int *)a.preempt))
                     ci = atomicAdd(a.work, 1ull);
                 ci = __shfl_sync(0xffffffffu, ci, 0);
                 if (ci >= a.n_chunks) {

@@ -31,7 +31,13 @@ struct ExpandArgs {
     unsigned int *inst_unique;       // per instance: new keys claimed
     unsigned long long *n_raw;       // children produced (all instances)
     unsigned int *status;
-    unsigned long long *work;        // dynamic chunk counter, zeroed before launch
+    unsigned long long *work;        // dynamic chunk counter, zeroed before the row's first launch
+    // Cooperative preemption (nullptr = none): while *preempt is nonzero
+    // (host memory mapped into the device), warps take no new chunk, finish
+    // the items they hold and exit.  The launch then ends with *work <
+    // n_chunks; launching again with the same arguments (counters kept)
+    // processes the chunks not yet taken.
+    const unsigned int *preempt;
     unsigned int max_probe;
     uint32_t prefetch;               // request each child's table line into L2 when staged
     // Single-instance launches (one segment): the instance's n_plc

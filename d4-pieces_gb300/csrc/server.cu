@@ -10,7 +10,11 @@
 //                per SM free, so fast-lane kernels run beside it, and while
 //                the fast lane has work each slow-lane row step waits (up
 //                to kSlowYieldMs) for it to go idle, so short requests get
-//                the GPU first.
+//                the GPU first.  A slow-lane k_expand started while the fast
+//                lane was idle is preempted when a request arrives: its
+//                warps take no new chunk (a flag in mapped host memory), the
+//                launch ends within about one chunk, and the row resumes
+//                once the fast lane is idle again (or kSlowYieldMs later).
 // A heavy request therefore never holds up the rows of the light ones, and
 // both lanes' launches overlap on the device.  Each lane loop admits queued
 // requests in arrival order while the projected device bytes of everything
@@ -68,6 +72,15 @@ constexpr uint64_t kFastStates = 1ull << 17;
 // req/s 293 -> 344 puzzles/s (no wait vs 10 ms).
 constexpr double kSlowYieldMs = 10.0;
 
+// Slow-lane launch plan: chunks per resident warp (the default plan aims at
+// 8), so that a preempted k_expand ends within a few percent of its length.
+constexpr uint32_t kSlowChunksPerWarp = 32;
+
+bool server_preempt() {
+    const char *v = std::getenv("D4E_PREEMPT");
+    return !(v && std::strcmp(v, "0") == 0);
+}
+
 bool server_autotune() {
     const char *v = std::getenv("D4E_SERVER_AUTOTUNE");
     return v && std::strcmp(v, "1") == 0;
@@ -103,6 +116,16 @@ public:
                                       : std::min<uint64_t>(150ull << 30, cap);
         int occ = 0;
         cuda_check(expand_max_blocks_per_sm(true, &occ), "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        if (const char *v = std::getenv("D4E_SLOW_YIELD_MS"))
+            slow_yield_ms_ = std::atof(v);
+        if (server_preempt() && slow_yield_ms_ > 0) {
+            void *h = nullptr;
+            cuda_check(cudaHostAlloc(&h, sizeof(unsigned int), cudaHostAllocMapped), "cudaHostAlloc");
+            preempt_h_.reset(static_cast<unsigned int *>(h));
+            *preempt_h_ = 0;
+            cuda_check(cudaHostGetDevicePointer(reinterpret_cast<void **>(&preempt_d_), h, 0),
+                       "cudaHostGetDevicePointer");
+        }
         for (int l = 0; l < 2; l++) {
             Lane &ln = lane_[l];
             EngineOpts eo;
@@ -116,6 +139,11 @@ public:
             eo.autotune = server_autotune();
             if (l == 1 && occ > 1)
                 eo.expand_ctas_per_sm = occ - 1;
+            if (l == 1 && preempt_d_) {
+                eo.preempt_flag = preempt_d_;
+                eo.preempt_gate = [this](bool preempted) { return slow_gate(preempted); };
+                eo.chunks_per_warp = kSlowChunksPerWarp;
+            }
             EngineOpts e64 = eo;
             e64.k64_inst_bits = kServerIdBits;
             ln.eng[0] = std::make_unique<Engine>(e64);
@@ -123,8 +151,6 @@ public:
             e128.key_mode = KeyMode::K128;
             ln.eng[1] = std::make_unique<Engine>(e128);
         }
-        if (const char *v = std::getenv("D4E_SLOW_YIELD_MS"))
-            slow_yield_ms_ = std::atof(v);
         if (const char *v = std::getenv("D4E_FAST_STATES"))
             fast_states_ = std::max<uint64_t>(1, std::strtoull(v, nullptr, 10));
         for (int l = 0; l < 2; l++)
@@ -170,6 +196,7 @@ public:
                 throw Error(worker_code_, worker_msg_);
             lane_[0].queue.push_back(std::move(r));
             st_.submitted++;
+            set_fast_busy(true);
         }
         lane_[0].cv.notify_all();
     }
@@ -249,13 +276,13 @@ private:
                     // Short requests first: while the fast lane has work, the
                     // slow lane holds its next row step back (at most
                     // slow_yield_ms_ per step), so fast-lane rows get the
-                    // whole GPU; heavy requests progress in the gaps.
+                    // whole GPU; heavy requests progress in the gaps.  A step
+                    // that starts with the fast lane idle may be preempted.
                     std::unique_lock<std::mutex> lk(mu_);
-                    yield_cv_.wait_for(lk, std::chrono::duration<double, std::milli>(slow_yield_ms_),
-                                       [&] {
-                                           return stop_ || (lane_[0].n_running == 0 &&
-                                                            lane_[0].queue.empty());
-                                       });
+                    const bool idle = yield_cv_.wait_for(
+                        lk, std::chrono::duration<double, std::milli>(slow_yield_ms_),
+                        [&] { return stop_ || fast_idle(); });
+                    slow_preemptible_ = idle && !stop_;
                 }
                 bool busy = false;
                 for (int e = 0; e < 2; e++) {
@@ -291,6 +318,7 @@ private:
                     st_.lane_kernel_ms[l] += s.expand_ms + s.compact_ms;
                     st_.lane_inst_rows[l] += n_run - s.paused;
                     st_.restarts += ln.eng[e]->totals().restarts - restarts0;
+                    st_.preemptions += after.preemptions - before.preemptions;
                     st_.paused += s.paused;
                 }
                 if (l == 0)
@@ -303,8 +331,11 @@ private:
                 ln.projected = proj;
                 if (stop_)
                     return;
-                if (!busy && ln.queue.empty())
+                if (!busy && ln.queue.empty()) {
+                    if (l == 0)
+                        set_fast_busy(false);
                     ln.cv.wait(lk, [&] { return stop_ || !ln.queue.empty(); });
+                }
                 if (stop_)
                     return;
             }
@@ -399,6 +430,30 @@ private:
         }
     }
 
+    // Guarded by mu_.
+    bool fast_idle() const { return lane_[0].n_running == 0 && lane_[0].queue.empty(); }
+
+    // The preemption flag the slow lane's k_expand polls: set while the fast
+    // lane has requests (guarded by mu_).
+    void set_fast_busy(bool busy) {
+        if (preempt_h_)
+            __atomic_store_n(preempt_h_.get(), busy ? 1u : 0u, __ATOMIC_RELEASE);
+    }
+
+    // Called by the slow lane's engines before each k_expand launch: whether
+    // the launch may be preempted.  After a preemption it first waits for the
+    // fast lane to go idle (at most slow_yield_ms_); a fast lane still busy
+    // then gets no second preemption of the same row.
+    bool slow_gate(bool preempted) {
+        std::unique_lock<std::mutex> lk(mu_);
+        if (!preempted)
+            return slow_preemptible_ && !stop_;
+        const bool idle = yield_cv_.wait_for(
+            lk, std::chrono::duration<double, std::milli>(slow_yield_ms_),
+            [&] { return stop_ || fast_idle(); });
+        return idle && !stop_;
+    }
+
     void collect(int l, int e) {
         Lane &ln = lane_[l];
         Engine &eng = *ln.eng[e];
@@ -458,11 +513,18 @@ private:
 
     d4e_server_opts opts_;
     uint64_t budget_ = 0;
+    struct FreeHost {
+        void operator()(unsigned int *p) const { cudaFreeHost(p); }
+    };
+    // Preemption flag (mapped host memory); outlives the lanes' engines.
+    std::unique_ptr<unsigned int, FreeHost> preempt_h_;
     Lane lane_[2];
     std::mutex mu_;
     std::condition_variable done_cv_;
     std::condition_variable yield_cv_;   // fast lane stepped (slow lane may go)
     double slow_yield_ms_ = kSlowYieldMs;
+    bool slow_preemptible_ = false;          // guarded by mu_
+    unsigned int *preempt_d_ = nullptr;      // device address of the preemption flag
     uint64_t fast_states_ = kFastStates;   // fast-lane row limit (D4E_FAST_STATES overrides)
     std::deque<d4e_result> results_;
     d4e_server_stats st_{};

@@ -165,6 +165,7 @@ class ServerStats(C.Structure):
         ("lane_solve_one_ms", C.c_double * 2),
         ("lane_retries", C.c_uint64 * 2),
         ("lane_phase_ms", (C.c_double * 6) * 2),
+        ("preemptions", C.c_uint64),
     ]
 
     def as_dict(self) -> dict:

@@ -366,6 +366,7 @@ typedef struct d4e_server_stats {
     double lane_solve_one_ms[2];/* per lane, inside steps: keeping levels + tracing */
     uint64_t lane_retries[2];   /* per lane: table-region overflows redone */
     double lane_phase_ms[2][6]; /* per lane: the row-step phases of d4e_stats.phase_ms */
+    uint64_t preemptions;       /* slow-lane k_expand launches ended early for the fast lane */
 } d4e_server_stats;
 
 int d4e_server_stats_get(d4e_server *s, d4e_server_stats *st);

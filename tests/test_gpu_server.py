@@ -100,3 +100,41 @@ def test_server_rejects_bad_requests_without_stopping(E):
         srv.close()
     assert got[1]["status"] != 0
     assert got[2]["status"] == 0 and got[2]["count"] == 5
+
+
+def test_server_preempted_rows_keep_results(E, oracle):
+    """Small requests arriving while the 8x15 enumeration runs in the slow
+    lane preempt its k_expand launches (warps stop taking chunks, the row
+    resumes later): the enumeration still gives the oracle's pinned count,
+    and every small request its result alone."""
+    import json
+
+    from conftest import GOLDEN
+    from d4gb.problem import Problem
+
+    c = next(c for c in json.loads((GOLDEN / "large.json").read_text())["cases"]
+             if c["name"].startswith("single large"))
+    big = Problem(c["width"], c["height"], list(c["rows"]), c["shapes"], c["counts"], c["sym"],
+                  name=c["name"])
+    probs, modes = mix_requests(40, 57)
+    beam = 128
+    want = alone_results(E, probs, modes, beam)
+    srv = E.Server(beam=beam)
+    try:
+        srv.submit(big, 0, 1000)
+        t0 = time.time()
+        while srv.stats()["moved"] == 0 and time.time() - t0 < 60:
+            time.sleep(0.005)
+        time.sleep(0.05)
+        for i, (p, m) in enumerate(zip(probs, modes)):
+            srv.submit(p, m, i)
+            time.sleep(0.01)
+        srv.drain(600)
+        got = {r["tag"]: r for r in srv.poll(1000)}
+        st = srv.stats()
+    finally:
+        srv.close()
+    assert got[1000]["status"] == 0 and got[1000]["count"] == int(c["count"])
+    for i, p in enumerate(probs):
+        assert same(got[i], want[i]), (p.name, got[i], want[i])
+    assert st["preemptions"] > 0
