@@ -787,10 +787,17 @@ StepStats Engine::step_impl() {
     std::sort(order.begin(), order.end());
     std::vector<uint32_t> run, paused;
     double paused_bytes = 0, run_front = 0, run_table = 0;
-    for (uint32_t id : order)
+    bool any_free = false;
+    for (uint32_t id : order) {
         paused_bytes += (double)inst_[id].seg_len * rec_bytes;
+        any_free |= !inst_[id].held;
+    }
     for (uint32_t id : order) {
         const Inst &in = inst_[id];
+        if (in.held && any_free) {
+            paused.push_back(id);
+            continue;
+        }
         const double est = (double)std::max<uint64_t>(in.seg_len, 1) * in.growth;
         const double f = est * rec_bytes, t = est / tune_.load * (double)slot_bytes;
         const double seg_b = (double)in.seg_len * rec_bytes;

@@ -251,6 +251,9 @@ public:
     const PieceSets &sets(uint32_t id) const { return inst_.at(id).sets; }
     // Frees a finished instance's id for reuse by a later add().
     void release(uint32_t id);
+    // A held instance sits out the following steps (its frontier carried
+    // unchanged) while some active instance is not held.
+    void set_hold(uint32_t id, bool hold) { inst_.at(id).held = hold; }
     const std::vector<uint64_t> &level_sizes(uint32_t id) const { return inst_.at(id).level_sizes; }
     uint64_t next_size_estimate(uint32_t id) const;
     // States of the instance's frontier whose current row equals `pattern`.
@@ -278,6 +281,7 @@ private:
         uint32_t width = 0, height = 0;
         uint32_t row = 0;
         bool active = false, done = false, result_ready = false;
+        bool held = false;
         uint64_t seg_begin = 0, seg_len = 0;
         uint64_t result = 0;
         std::vector<uint64_t> level_sizes;

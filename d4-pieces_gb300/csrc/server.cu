@@ -15,6 +15,9 @@
 //                warps take no new chunk (a flag in mapped host memory), the
 //                launch ends within about one chunk, and the row resumes
 //                once the fast lane is idle again (or kSlowYieldMs later).
+//                Requests here differ in row cost by orders of magnitude:
+//                the heavy ones sit out some row steps (see plan_share), so
+//                the lighter ones are not paced by the heaviest row.
 // A heavy request therefore never holds up the rows of the light ones, and
 // both lanes' launches overlap on the device.  Each lane loop admits queued
 // requests in arrival order while the projected device bytes of everything
@@ -75,6 +78,17 @@ constexpr double kSlowYieldMs = 10.0;
 // Slow-lane launch plan: chunks per resident warp (the default plan aims at
 // 8), so that a preempted k_expand ends within a few percent of its length.
 constexpr uint32_t kSlowChunksPerWarp = 32;
+
+// Slow-lane sharing: requests whose next row is projected at more than this
+// many times the cheapest running one's sit out some row steps.
+constexpr double kShareRatio = 8.0;
+
+// Time of the steps without the heavy requests per step with them
+// (D4E_SLOW_SHARE overrides; 0 = no sharing).
+double server_share() {
+    const char *v = std::getenv("D4E_SLOW_SHARE");
+    return v ? std::max(0.0, std::atof(v)) : 1.0;
+}
 
 bool server_preempt() {
     const char *v = std::getenv("D4E_PREEMPT");
@@ -240,6 +254,9 @@ private:
         double projected = 0;                                 // guarded by mu_
         double avg_peak = 0;                                  // worker-owned
         uint64_t n_peaks = 0;
+        // Slow-lane sharing, per engine: time of the last step that ran
+        // every request, and of the steps without the heavy ones since.
+        double last_full_ms[2] = {0, 0}, owed_ms[2] = {0, 0};
     };
 
     // Bytes charged for a request not yet started: solve-one requests are
@@ -293,8 +310,15 @@ private:
                     const Totals before = ln.eng[e]->totals();
                     const uint64_t restarts0 = before.restarts;
                     const size_t n_run = ln.running[e].size();
+                    const bool held = l == 1 && share_ > 0 && plan_share(ln, e);
                     const StepStats s = ln.eng[e]->step();
                     const auto t1 = Clock::now();
+                    if (held) {
+                        ln.owed_ms[e] += ms_between(t0, t1);
+                    } else if (l == 1) {
+                        ln.last_full_ms[e] = ms_between(t0, t1);
+                        ln.owed_ms[e] = 0;
+                    }
                     collect(l, e);
                     const auto t2 = Clock::now();
                     const Totals &after = ln.eng[e]->totals();
@@ -430,6 +454,30 @@ private:
         }
     }
 
+    // Sharing in the slow lane: one row step advances every running request,
+    // and requests that outgrew the fast lane differ in row cost by orders of
+    // magnitude.  While some running requests' next rows are projected at
+    // more than kShareRatio times the cheapest one's, those heavy ones sit
+    // out row steps until the steps without them have taken as long as the
+    // last step with them: the others move at their own pace, and the heavy
+    // ones keep about half of the lane's time.  Returns whether any request
+    // sits out the next step.
+    bool plan_share(Lane &ln, int e) {
+        Engine &eng = *ln.eng[e];
+        uint64_t cheapest = UINT64_MAX;
+        for (const auto &[id, r] : ln.running[e])
+            cheapest = std::min<uint64_t>(cheapest, std::max<uint64_t>(eng.projected_bytes(id), 1));
+        const bool light_turn = ln.owed_ms[e] < share_ * ln.last_full_ms[e];
+        bool any = false;
+        for (const auto &[id, r] : ln.running[e]) {
+            const bool hold = light_turn && (double)eng.projected_bytes(id) >
+                                                kShareRatio * (double)cheapest;
+            eng.set_hold(id, hold);
+            any |= hold;
+        }
+        return any;
+    }
+
     // Guarded by mu_.
     bool fast_idle() const { return lane_[0].n_running == 0 && lane_[0].queue.empty(); }
 
@@ -524,6 +572,7 @@ private:
     std::condition_variable yield_cv_;   // fast lane stepped (slow lane may go)
     double slow_yield_ms_ = kSlowYieldMs;
     bool slow_preemptible_ = false;          // guarded by mu_
+    double share_ = server_share();          // slow-lane sharing (0: off)
     unsigned int *preempt_d_ = nullptr;      // device address of the preemption flag
     uint64_t fast_states_ = kFastStates;   // fast-lane row limit (D4E_FAST_STATES overrides)
     std::deque<d4e_result> results_;
