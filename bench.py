@@ -966,6 +966,16 @@ def serve_section(E, dev: int, rate: float, seconds: float, max_states: int, bea
     for i in set(rs) & set(rp):
         if rs[i][0] == 0 and rp[i][0] == 0 and rs[i] != rp[i]:
             raise RuntimeError(f"request {i}: served and plain results differ")
+    # Error statuses per arm, and the requests that failed in one arm only.
+    for arm, res, other in (("served", rs, rp), ("plain", rp, rs)):
+        hist = {}
+        for r in res.values():
+            if r[0]:
+                hist[str(r[0])] = hist.get(str(r[0]), 0) + 1
+        arm_d = served if arm == "served" else plain
+        arm_d["failed_status"] = hist
+        arm_d["failed_here_only"] = sum(1 for i in set(res) & set(other)
+                                        if res[i][0] and not other[i][0])
     load = (rate * plain["mean_service_ms"] / 1e3) if plain["mean_service_ms"] else None
     return {"rate_req_s": rate, "arrival_window_s": seconds, "requests": len(arr),
             "grace_s": grace, "offered_load_vs_plain_capacity": load,

@@ -5,6 +5,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <new>
 #include <string>
@@ -305,7 +306,24 @@ int d4e_searcher_solutions(d4e_searcher *s, uint64_t max, int32_t single, int8_t
     return guarded([&] {
         if (!s || !n)
             return fail(D4E_ERR_INVALID, "null pointer");
-        *n = s->eng->solutions(s->id, max, type_grids, step_grids, single != 0);
+        // Step numbers come as int16 (boards of up to 512 cells); this
+        // interface's grids are int8, like the reference's Step::piece_id.
+        std::vector<int16_t> steps;
+        if (step_grids) {
+            const uint64_t cells = (uint64_t)s->eng->width(s->id) * s->eng->height(s->id);
+            const bool ok = s->eng->done(s->id) && !s->eng->status(s->id);
+            uint64_t rows = std::min<uint64_t>(max, ok ? s->eng->count(s->id) : 0);
+            if (single != 0)
+                rows = std::min<uint64_t>(rows, 1);
+            steps.resize(rows * cells);
+        }
+        *n = s->eng->solutions(s->id, max, type_grids, step_grids ? steps.data() : nullptr,
+                               single != 0);
+        if (step_grids) {
+            const uint64_t cells = (uint64_t)s->eng->width(s->id) * s->eng->height(s->id);
+            for (uint64_t k = 0; k < *n * cells; k++)
+                step_grids[k] = (int8_t)steps[k];
+        }
         return D4E_OK;
     });
 }
@@ -446,6 +464,7 @@ d4e::InstanceSpec to_spec(const d4e_instance &in, uint32_t mode, uint64_t max_st
     sp.sym = in.sym;
     sp.mode = mode == D4E_MODE_SOLVE_ONE ? d4e::Mode::SolveOne
               : mode == D4E_MODE_SETS    ? d4e::Mode::Sets
+              : mode == D4E_MODE_LIST    ? d4e::Mode::List
                                          : d4e::Mode::Count;
     sp.max_states = max_states;
     sp.beam = beam;
@@ -499,21 +518,28 @@ void d4e_release_cached_memory(void) { d4e::release_idle_pools(); }
 
 namespace {
 
-// The batch runner behind d4e_batch_run and d4e_batch_sets; `sets`
-// receives each instance's piece multisets in Sets mode.
+// Called for each finished instance of a batch before its engine goes away
+// (engine, engine id, instance index).
+using BatchHook = std::function<void(d4e::Engine &, uint32_t, uint32_t)>;
+
+// The batch runner behind d4e_batch_run, d4e_batch_sets and
+// d4e_batch_solutions; `sets` receives each instance's piece multisets in
+// Sets mode, `hook` (list mode) sees each finished instance.
 int batch_impl(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
                d4e_result *results, d4e_stats *st,
-               std::vector<d4e::PieceSets> *sets) {
+               std::vector<d4e::PieceSets> *sets, const BatchHook &hook = nullptr) {
     return guarded([&] {
         if ((!insts && n) || (!results && n))
             return fail(D4E_ERR_INVALID, "null pointer");
         const d4e_batch_opts o = opts ? *opts : d4e_batch_opts{};
-        if (o.mode > D4E_MODE_SETS)
-            return fail(D4E_ERR_INVALID, "unknown mode");
+        if (o.mode > D4E_MODE_LIST || (o.mode == D4E_MODE_LIST) != (bool)hook)
+            return fail(D4E_ERR_INVALID, o.mode == D4E_MODE_LIST
+                                             ? "list mode runs through d4e_batch_solutions"
+                                             : "unknown mode");
         for (uint32_t i = 0; i < n; i++)
             if (insts[i].width * insts[i].height > sizeof(results[i].grid) &&
-                o.mode == D4E_MODE_SOLVE_ONE)
-                return fail(D4E_ERR_INVALID, "solve-one boards are limited to 512 cells");
+                (o.mode == D4E_MODE_SOLVE_ONE || o.mode == D4E_MODE_LIST))
+                return fail(D4E_ERR_INVALID, "solve-one and list boards are limited to 512 cells");
         if (sets)
             sets->assign(n, {});
         const auto t0 = std::chrono::steady_clock::now();
@@ -521,6 +547,8 @@ int batch_impl(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts
             d4e::engine_result(eng, id, o.mode, &results[i]);
             if (sets && results[i].status == 0)
                 (*sets)[i] = eng.sets(id);
+            if (hook && results[i].status == 0)
+                hook(eng, id, i);
             results[i].tag = i;
             results[i].queued_ms = 0;
             results[i].latency_ms =
@@ -641,6 +669,62 @@ int d4e_batch_sets(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *
                             nt);
                 set_tilings[k] = ps.tilings[j];
             }
+        }
+        return D4E_OK;
+    });
+}
+
+int d4e_batch_solutions(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
+                        uint64_t max_per_instance, d4e_result *results, uint64_t *sol_offsets,
+                        int8_t *type_grids, int16_t *step_grids, uint64_t max_total,
+                        d4e_stats *st) {
+    d4e_batch_opts o = opts ? *opts : d4e_batch_opts{};
+    o.mode = D4E_MODE_LIST;
+    o.beam = 0;
+    if (n && !sol_offsets)
+        return fail(D4E_ERR_INVALID, "null pointer");
+    // Each instance's tilings are reconstructed while its engine still holds
+    // its rows, into host buffers of D4E_GRID_CELLS cells per tiling.
+    std::vector<std::vector<int8_t>> tg(n);
+    std::vector<std::vector<int16_t>> sg(n);
+    std::vector<uint64_t> got(n, 0);
+    const BatchHook hook = [&](d4e::Engine &eng, uint32_t id, uint32_t i) {
+        const uint64_t cells = (uint64_t)eng.width(id) * eng.height(id);
+        const uint64_t want = std::min<uint64_t>(max_per_instance, eng.count(id));
+        if (!want)
+            return;
+        std::vector<int8_t> t(want * cells);
+        std::vector<int16_t> sp(want * cells);
+        got[i] = eng.solutions(id, want, t.data(), sp.data(), false);
+        tg[i].assign(got[i] * D4E_GRID_CELLS, -1);
+        sg[i].assign(got[i] * D4E_GRID_CELLS, -1);
+        for (uint64_t k = 0; k < got[i]; k++) {
+            std::memcpy(tg[i].data() + k * D4E_GRID_CELLS, t.data() + k * cells, cells);
+            std::memcpy(sg[i].data() + k * D4E_GRID_CELLS, sp.data() + k * cells,
+                        cells * sizeof(int16_t));
+        }
+    };
+    const int rc = batch_impl(insts, n, &o, results, st, nullptr, hook);
+    if (rc != D4E_OK)
+        return rc;
+    return guarded([&] {
+        uint64_t total = 0;
+        for (uint32_t i = 0; i < n; i++) {
+            sol_offsets[i] = total;
+            total += got[i];
+        }
+        sol_offsets[n] = total;
+        if (total > max_total)
+            return fail(D4E_ERR_INVALID, "max_total too small: " + std::to_string(total) +
+                                             " tilings (sol_offsets[n])");
+        if (total && (!type_grids || !step_grids))
+            return fail(D4E_ERR_INVALID, "null pointer");
+        for (uint32_t i = 0; i < n; i++) {
+            if (!got[i])
+                continue;
+            std::memcpy(type_grids + sol_offsets[i] * D4E_GRID_CELLS, tg[i].data(), tg[i].size());
+            std::memcpy(step_grids + sol_offsets[i] * D4E_GRID_CELLS, sg[i].data(),
+                        sg[i].size() * sizeof(int16_t));
         }
         return D4E_OK;
     });

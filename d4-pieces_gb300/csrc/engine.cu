@@ -357,8 +357,8 @@ uint32_t Engine::add(const InstanceSpec &sp) {
     if (inst_.size() >= kMaxInstances)
         throw Error(kErrUnsupported, "too many instances");
 
-    if (sp.mode == Mode::SolveOne && opts_.keep_levels)
-        throw Error(kErrInvalid, "solve-one instances need an engine without keep_levels");
+    if ((sp.mode == Mode::SolveOne || sp.mode == Mode::List) && opts_.keep_levels)
+        throw Error(kErrInvalid, "solve-one and list instances need an engine without keep_levels");
 
     Inst in;
     const std::string err = build_piece_lib(sp.shapes, sp.counts, sp.n_pieces, sp.sym, sp.width,
@@ -742,10 +742,10 @@ StepStats Engine::step_impl() {
         n_cur_ += rk.size();
         std::vector<uint32_t> roots;
         for (uint32_t id : pending_)
-            if (inst_[id].mode == Mode::SolveOne)
+            if (inst_[id].mode == Mode::SolveOne || inst_[id].mode == Mode::List)
                 roots.push_back(id);
         pending_.clear();
-        keep_levels_of(roots);   // level 0 of solve-one instances
+        keep_levels_of(roots);   // level 0 of solve-one and list instances
     }
     tot_.upload_ms += host_ms_since(t_up);
     if (n_active_ == 0)
@@ -1480,20 +1480,20 @@ StepStats Engine::step_impl() {
     // Advance the instances.
     std::vector<uint32_t> still;
     still.reserve(active_.size());
-    std::vector<uint32_t> keep_now, to_trace, ended;
+    std::vector<uint32_t> keep_now, to_trace, to_total, ended;
     for (const auto &[id, begin] : nseg) {
         Inst &in = inst_[id];
         in.seg_begin = begin;
         in.seg_len = h_unique_[id];
         in.level_sizes.push_back(in.seg_len);
         in.row++;
-        if (in.mode == Mode::SolveOne) {
+        if (in.mode == Mode::SolveOne || in.mode == Mode::List) {
             if (in.seg_len == 0) {
                 ended.push_back(id);
             } else {
                 keep_now.push_back(id);
                 if (in.row == in.height)
-                    to_trace.push_back(id);
+                    (in.mode == Mode::SolveOne ? to_trace : to_total).push_back(id);
                 else
                     still.push_back(id);
             }
@@ -1619,6 +1619,7 @@ StepStats Engine::step_impl() {
     const auto t_trace = HostClock::now();
     tot_.keep_ms += host_ms_since(t_keep);
     trace_solutions(to_trace);
+    total_lists(to_total);
     tot_.trace_ms += host_ms_since(t_trace);
     for (uint32_t id : ended) {
         if (inst_[id].sampled)
@@ -1910,6 +1911,42 @@ void Engine::finish_solve_one(uint32_t id, bool found) {
     n_active_--;
 }
 
+void Engine::total_lists(const std::vector<uint32_t> &ids) {
+    // A list instance's tilings: the counts of its final level, which stays
+    // kept (with every other level) for solutions().
+    for (uint32_t id : ids) {
+        Inst &in = inst_[id];
+        const LevelRef &l = in.levels.back();
+        const LvlChunk &c = chunks_[l.chunk];
+        unsigned long long sum = 0;
+        if (k64_) {
+            std::vector<ulonglong2> rec(l.len);
+            cuda_check(cudaMemcpyAsync(rec.data(), c.keys + l.first, l.len * sizeof(ulonglong2),
+                                       cudaMemcpyDeviceToHost, stream_),
+                       "read final level");
+            cuda_check(cudaStreamSynchronize(stream_), "read final level");
+            for (const auto &r : rec)
+                sum += r.y;
+        } else {
+            std::vector<unsigned long long> cn(l.len);
+            cuda_check(cudaMemcpyAsync(cn.data(), c.cnts + l.first,
+                                       l.len * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                       stream_),
+                       "read final level");
+            cuda_check(cudaStreamSynchronize(stream_), "read final level");
+            for (auto v : cn)
+                sum += v;
+        }
+        tot_.d2h_bytes += l.len * (k64_ ? 16 : 8);
+        in.result = sum;
+        in.result_ready = true;
+        in.active = false;
+        in.done = true;
+        in.seg_len = 0;
+        n_active_--;
+    }
+}
+
 void Engine::restart(uint32_t id) {
     // The sampled attempt ended without a tiling: start again from the
     // root with a 16x wider sample (exact from 2^24 states on).
@@ -2116,25 +2153,44 @@ uint64_t Engine::count(uint32_t id) {
     return in.result;
 }
 
-uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t *step_grids,
+uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int16_t *step_grids,
                            bool single) {
     EngineScope g(opts_.device, &pool_);
-    if (!opts_.keep_levels)
-        throw Error(kErrState, "solutions need an engine created with keep_levels");
     Inst &in = inst_.at(id);
+    if (!opts_.keep_levels && in.mode != Mode::List)
+        throw Error(kErrState,
+                    "solutions need an engine created with keep_levels, or a list instance");
     if (!in.done)
         throw Error(kErrState, "instance has not finished");
     const uint32_t H = in.height;
     if (in.row < H || count(id) == 0 || max == 0)
         return 0;
-    if (lvl_n_.size() != (size_t)H + 1)
-        throw Error(kErrState, "level store incomplete");
+    // The instance's levels: the engine's level store (keep_levels), or the
+    // rows kept for this list instance.
+    std::vector<ulonglong2 *> lk(H + 1, nullptr);
+    std::vector<uint64_t> ln(H + 1, 0);
+    if (opts_.keep_levels) {
+        if (lvl_n_.size() != (size_t)H + 1)
+            throw Error(kErrState, "level store incomplete");
+        for (uint32_t r = 0; r <= H; r++) {
+            lk[r] = lvl_keys_[r];
+            ln[r] = lvl_n_[r];
+        }
+    } else {
+        if (in.levels.size() != (size_t)H + 1)
+            throw Error(kErrState, "list level store incomplete");
+        for (uint32_t r = 0; r <= H; r++) {
+            const LevelRef &l = in.levels[r];
+            lk[r] = chunks_[l.chunk].keys + l.first;
+            ln[r] = l.len;
+        }
+    }
 
     // Backward pass: live[r] = states of level r with a child in live[r + 1].
     std::vector<ulonglong2 *> live(H + 1, nullptr);
     std::vector<uint64_t> live_n(H + 1, 0);
-    live[H] = lvl_keys_[H];
-    live_n[H] = lvl_n_[H];
+    live[H] = lk[H];
+    live_n[H] = ln[H];
     DevBuf<unsigned char> alive;
     DevBuf<unsigned long long> nsel;
     nsel.reserve(1, stream_);
@@ -2180,15 +2236,15 @@ uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t
     };
     for (int r = (int)H - 1; r >= 0; r--) {
         const uint64_t cap = build_set(live[r + 1], live_n[r + 1]);
-        const uint64_t n = lvl_n_[r];
+        const uint64_t n = ln[r];
         alive.reserve(std::max<uint64_t>(n, 1), stream_);
-        launch_mark_alive(k64_, probe_args((uint32_t)r, cap), lvl_keys_[r], n, alive.p, sms_ * 4,
+        launch_mark_alive(k64_, probe_args((uint32_t)r, cap), lk[r], n, alive.p, sms_ * 4,
                           stream_);
         ulonglong2 *out = nullptr;
         cuda_check(cudaMalloc(&out, std::max<uint64_t>(n, 1) * sizeof(ulonglong2)), "cudaMalloc");
         owned.push_back(out);
         cuda_check(cudaMemsetAsync(nsel.p, 0, sizeof(unsigned long long), stream_), "memset");
-        launch_select(lvl_keys_[r], alive.p, n, out, nsel.p, sms_ * 4, stream_);
+        launch_select(lk[r], alive.p, n, out, nsel.p, sms_ * 4, stream_);
         unsigned long long ns = 0;
         cuda_check(cudaMemcpyAsync(&ns, nsel.p, sizeof(ns), cudaMemcpyDeviceToHost, stream_),
                    "read select");
@@ -2203,7 +2259,7 @@ uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t
     PathNode root{};
     {
         ulonglong2 rk;
-        cuda_check(cudaMemcpyAsync(&rk, lvl_keys_[0], sizeof(rk), cudaMemcpyDeviceToHost, stream_),
+        cuda_check(cudaMemcpyAsync(&rk, lk[0], sizeof(rk), cudaMemcpyDeviceToHost, stream_),
                    "read root");
         cuda_check(cudaStreamSynchronize(stream_), "read root");
         root.k0 = rk.x;
@@ -2258,7 +2314,7 @@ uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t
             nd = r >= 2 ? &levels[r - 1][nd->parent] : nullptr;
         }
         int8_t *tg = type_grids ? type_grids + produced * cells : nullptr;
-        int8_t *sg = step_grids ? step_grids + produced * cells : nullptr;
+        int16_t *sg = step_grids ? step_grids + produced * cells : nullptr;
         for (uint32_t cidx = 0; cidx < cells; cidx++) {
             if (tg)
                 tg[cidx] = -1;
@@ -2278,7 +2334,7 @@ uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t
                         if (tg)
                             tg[cell] = (int8_t)lib.plc_type[pi];
                         if (sg)
-                            sg[cell] = (int8_t)step;
+                            sg[cell] = (int16_t)step;
                     }
                 }
             }

@@ -143,7 +143,9 @@ struct Tuning {
 // Count: tilings.  SolveOne: one tiling.  Sets: the piece multisets that
 // tile the board (the final row's used-copy counters), each with its number
 // of tilings.
-enum class Mode : uint32_t { Count = 0, SolveOne = 1, Sets = 2 };
+// List: the tilings themselves -- counting with every row's frontier kept
+// per instance, from which solutions() lists them.
+enum class Mode : uint32_t { Count = 0, SolveOne = 1, Sets = 2, List = 3 };
 
 // One piece multiset of a Sets instance: copies per input piece type.
 // Piece multisets of a Sets-mode instance: set k uses copies[k * n_types + t]
@@ -261,10 +263,12 @@ public:
     // Pulls the counts of instances finished since the last call.
     void sync_results();
 
-    // Solutions of a finished single-instance engine created with
-    // keep_levels.  Writes up to max grids; returns the number of tilings
-    // reconstructed (== the count unless max truncated it).
-    uint64_t solutions(uint32_t id, uint64_t max, int8_t *type_grids, int8_t *step_grids,
+    // Solutions of a finished instance: the one instance of an engine
+    // created with keep_levels, or a Mode::List instance.  Writes up to max
+    // grids of width * height cells (piece types, placement numbers; -1 =
+    // not covered); returns the number of tilings reconstructed (== the
+    // count unless max truncated it).
+    uint64_t solutions(uint32_t id, uint64_t max, int8_t *type_grids, int16_t *step_grids,
                        bool single);
 
     const Totals &totals() const { return tot_; }
@@ -315,6 +319,7 @@ private:
     void drop_levels(Inst &in);
     void trace_solutions(const std::vector<uint32_t> &ids);
     void finish_solve_one(uint32_t id, bool found);
+    void total_lists(const std::vector<uint32_t> &ids);
     void restart(uint32_t id);
     uint64_t frontier_bytes(int buf) const;
     double memory_limit(double device_avail) const;

@@ -40,6 +40,7 @@ _u64p = C.POINTER(C.c_uint64)
 _u32p = C.POINTER(C.c_uint32)
 _u8p = C.POINTER(C.c_uint8)
 _i8p = C.POINTER(C.c_int8)
+_i16p = C.POINTER(C.c_int16)
 
 
 class D4Error(RuntimeError):
@@ -226,6 +227,8 @@ _sig("d4e_batch_run", C.c_int, C.POINTER(Instance), C.c_uint32, C.POINTER(BatchO
      C.POINTER(Result), C.POINTER(Stats))
 _sig("d4e_batch_sets", C.c_int, C.POINTER(Instance), C.c_uint32, C.POINTER(BatchOpts),
      C.POINTER(Result), _u64p, _u8p, _u64p, C.c_uint64, C.POINTER(Stats))
+_sig("d4e_batch_solutions", C.c_int, C.POINTER(Instance), C.c_uint32, C.POINTER(BatchOpts),
+     C.c_uint64, C.POINTER(Result), _u64p, _i8p, _i16p, C.c_uint64, C.POINTER(Stats))
 _sig("d4e_server_create", C.c_int, C.POINTER(ServerOpts), C.POINTER(C.c_void_p))
 _sig("d4e_server_submit", C.c_int, C.c_void_p, C.POINTER(Instance), C.c_uint32, C.c_uint64)
 _sig("d4e_server_poll", C.c_int, C.c_void_p, C.POINTER(Result), C.c_uint32, _u32p)
@@ -486,6 +489,46 @@ def batch_sets(problems, device: int = 0, memory_budget: int = 0, max_states: in
         a, b = int(offs[i]), int(offs[i + 1])
         rows = map(tuple, copies[a:b, : len(p.shapes)].tolist())
         out.append(list(zip(rows, til[a:b].tolist())))
+    return out, [res[i].as_dict() for i in range(n)], st.as_dict()
+
+
+MODE_LIST = 3
+GRID_CELLS = 512
+
+
+def batch_solutions(problems, max_per_instance: int = 1 << 16, device: int = 0,
+                    memory_budget: int = 0, max_states: int = 0, sequential: bool = False,
+                    wide_keys: bool = False, max_total: int = 1 << 16):
+    """Every tiling of every problem (d4e_batch_solutions): for each problem
+    a pair of arrays (type grids, step grids), each [tilings, height, width]
+    (piece type / placement number per cell, -1 = not covered), at most
+    max_per_instance tilings per problem; plus the results (count = all
+    tilings) and stats.  Runs once more with room for the number needed when
+    the batch lists more than max_total tilings."""
+    arr, keep = _instances(problems)
+    n = len(problems)
+    res = (Result * max(n, 1))()
+    flags = (D4E_BATCH_SEQUENTIAL if sequential else 0) | (D4E_BATCH_WIDE_KEYS if wide_keys else 0)
+    o = BatchOpts(MODE_LIST, flags, device, 0, memory_budget, max_states, 0)
+    offs = np.zeros(n + 1, dtype=np.uint64)
+    st = Stats()
+    while True:
+        tg = np.empty((max(max_total, 1), GRID_CELLS), dtype=np.int8)
+        sg = np.empty((max(max_total, 1), GRID_CELLS), dtype=np.int16)
+        rc = _lib.d4e_batch_solutions(arr, n, C.byref(o), max_per_instance, res,
+                                      offs.ctypes.data_as(_u64p), tg.ctypes.data_as(_i8p),
+                                      sg.ctypes.data_as(_i16p), max_total, C.byref(st))
+        if rc == D4E_ERR_INVALID and int(offs[n]) > max_total:
+            max_total = int(offs[n])
+            continue
+        _check(rc)
+        break
+    out = []
+    for i, p in enumerate(problems):
+        a, b = int(offs[i]), int(offs[i + 1])
+        cells = p.width * p.height
+        out.append((tg[a:b, :cells].reshape(b - a, p.height, p.width).copy(),
+                    sg[a:b, :cells].reshape(b - a, p.height, p.width).copy()))
     return out, [res[i].as_dict() for i in range(n)], st.as_dict()
 
 

@@ -249,6 +249,7 @@ int d4e_batch_count(const d4e_instance *insts, uint32_t n, uint32_t flags, int32
 #define D4E_MODE_SETS 2u       /* the piece multisets that tile the board (the pieces'
                                   counts are maxima), each with its number of tilings;
                                   results: count = all tilings, found = number of sets */
+#define D4E_MODE_LIST 3u       /* every tiling itself (d4e_batch_solutions only) */
 
 typedef struct d4e_batch_opts {
     uint32_t mode;              /* D4E_MODE_* for every instance */
@@ -305,6 +306,26 @@ int d4e_batch_run(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *o
 int d4e_batch_sets(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
                    d4e_result *results, uint64_t *set_offsets, uint8_t *set_copies,
                    uint64_t *set_tilings, uint64_t max_sets, d4e_stats *st);
+
+/* Lists the tilings of every instance of a batch: the reference's Solution /
+ * Step list (src/Piece.hpp:31-48, src/Piece.cpp:25-54; d4e_searcher_solutions
+ * for one board) for many boards in one run.  The instances advance together
+ * as in counting, each keeping every row's frontier on the device (device
+ * memory grows with the sum of all rows of all instances); each instance's
+ * tilings are then reconstructed from its own rows.  Instance i's tilings
+ * are sol_offsets[i] .. sol_offsets[i+1]-1 (at most max_per_instance, in no
+ * particular order); tiling k has piece type type_grids[k * D4E_GRID_CELLS + c]
+ * and placement number step_grids[k * D4E_GRID_CELLS + c] at cell c (row-major,
+ * width * height cells, -1 = not covered or beyond the board).
+ * results[i].count = all tilings of instance i.  sol_offsets has n + 1
+ * entries; when more than max_total tilings would be listed the call fails
+ * with D4E_ERR_INVALID and sol_offsets[n] holds the number needed.  Boards of
+ * up to 512 cells; opts->mode and opts->beam are ignored. */
+#define D4E_GRID_CELLS 512u
+int d4e_batch_solutions(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
+                        uint64_t max_per_instance, d4e_result *results, uint64_t *sol_offsets,
+                        int8_t *type_grids, int16_t *step_grids, uint64_t max_total,
+                        d4e_stats *st);
 
 /* ------------------------------------------------------------------------
  * Serving: a request loop on a native worker thread.  No counterpart in the
