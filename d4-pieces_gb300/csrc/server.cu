@@ -108,7 +108,12 @@ struct Request {
     uint64_t tag = 0;
     Clock::time_point t_submit, t_admit;
     bool moved = false;     // restarted in the slow lane
+    uint32_t nomem_retries = 0;
 };
+
+// A request that ran out of device memory while others shared the device
+// restarts in the slow lane (at most this many times) instead of failing.
+constexpr uint32_t kNoMemRetries = 2;
 
 }  // namespace
 
@@ -478,6 +483,12 @@ private:
         return any;
     }
 
+    // Whether more than one request is on the device.
+    bool shared_device() {
+        std::lock_guard<std::mutex> lk(mu_);
+        return lane_[0].n_running + lane_[1].n_running > 1;
+    }
+
     // Guarded by mu_.
     bool fast_idle() const { return lane_[0].n_running == 0 && lane_[0].queue.empty(); }
 
@@ -518,10 +529,17 @@ private:
         for (uint32_t id : fin) {
             Request &r = ln.running[e].at(id);
             // Outgrew the fast lane (and not the caller's own limit):
-            // restart in the slow lane.
-            if (l == 0 && eng.status(id) == kErrUnsupported &&
-                eng.error(id).rfind("frontier limit exceeded", 0) == 0 &&
-                (opts_.max_states == 0 || opts_.max_states > fast_states_)) {
+            // restart in the slow lane.  Out of device memory beside other
+            // requests: restart there too (a bounded number of times), since
+            // alone it may fit.
+            const bool outgrew = l == 0 && eng.status(id) == kErrUnsupported &&
+                                 eng.error(id).rfind("frontier limit exceeded", 0) == 0 &&
+                                 (opts_.max_states == 0 || opts_.max_states > fast_states_);
+            const bool crowded = eng.status(id) == kErrNoMem && r.nomem_retries < kNoMemRetries &&
+                                 shared_device();
+            if (outgrew || crowded) {
+                if (crowded)
+                    r.nomem_retries++;
                 r.moved = true;
                 moved.push_back(std::move(r));
             } else {
