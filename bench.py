@@ -67,7 +67,7 @@ def parse_args():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--seed", type=int, default=SINGLE_LARGE_SEED)
     ap.add_argument("--workload", choices=("single_large", "medium", "batched", "batched_one",
-                                           "serve", "family"),
+                                           "serve", "family", "list"),
                     default="single_large",
                     help="medium = 8x10 board, 78 cells, 16 pieces (profiling case: frontier "
                          "of ~18M states, a few hundred MB -- larger than L2, a few GB at most)")
@@ -640,6 +640,63 @@ def bench_batched(args, dist: Dist) -> None:
         }), flush=True)
 
 
+LIST_MAX_CELLS = 40
+LIST_PER_INSTANCE = 64
+
+
+def bench_list(args, dist: Dist) -> None:
+    """Batched solution listing: the tilings of the batched mix's boards of
+    at most LIST_MAX_CELLS cells (up to LIST_PER_INSTANCE per board), once
+    as one batch (d4e_batch_solutions) and once one board at a time through
+    the same call.  Counts must agree; boards with at most
+    LIST_PER_INSTANCE tilings must list the same tilings in both arms; every
+    listed tiling passes the independent cover check."""
+    from d4gb import engine as E
+    from d4gb.problem import batched_mix, verify_tiling
+
+    probs = [p for p in batched_mix(BATCHED_SEED, 16 * args.instances)
+             if p.cells <= LIST_MAX_CELLS][: args.instances]
+    res, outs = {}, {}
+    for arm, seq in (("batched", False), ("plain", True)):
+        t0 = time.perf_counter()
+        grids, out, st = E.batch_solutions(probs, max_per_instance=LIST_PER_INSTANCE,
+                                           device=dist.local_rank, sequential=seq)
+        wall = time.perf_counter() - t0
+        outs[arm] = (grids, out)
+        listed = sum(len(g[0]) for g in grids)
+        res[arm] = {"wall_s": wall, "puzzles_per_s": len(probs) / wall,
+                    "tilings_listed": listed, "tilings_per_s": listed / wall,
+                    "expand_launches": st["expand_launches"],
+                    "other_launches": st["other_launches"], "states": st["states_out"]}
+    (gb, ob), (gp, op) = outs["batched"], outs["plain"]
+    for i, p in enumerate(probs):
+        if (ob[i]["status"], ob[i]["count"]) != (op[i]["status"], op[i]["count"]):
+            raise RuntimeError(f"board {i}: batched and plain counts differ")
+        if ob[i]["count"] <= LIST_PER_INSTANCE:
+            a = {(t.tobytes(), s_.tobytes()) for t, s_ in zip(*gb[i])}
+            b = {(t.tobytes(), s_.tobytes()) for t, s_ in zip(*gp[i])}
+            if a != b:
+                raise RuntimeError(f"board {i}: batched and plain tilings differ")
+        for t, s_ in zip(*gb[i]):
+            if not verify_tiling(p, t, s_):
+                raise RuntimeError(f"board {i}: a listed tiling fails the cover check")
+    if dist.rank == 0:
+        print(json.dumps({
+            "metric": "puzzles/s (batched solution listing)",
+            "value": res["batched"]["puzzles_per_s"],
+            "unit": "puzzles/s",
+            "n_gpus": dist.world,
+            "config": {"workload": f"batched mix boards of at most {LIST_MAX_CELLS} cells: "
+                                   f"{len(probs)} boards, seed {BATCHED_SEED}, up to "
+                                   f"{LIST_PER_INSTANCE} tilings listed per board"},
+            "boards_with_tilings": sum(1 for r in ob if r["count"]),
+            "tilings_total": sum(r["count"] for r in ob),
+            "batched": res["batched"], "plain": res["plain"],
+            "speedup_vs_plain": res["batched"]["puzzles_per_s"] / res["plain"]["puzzles_per_s"],
+            "cover_checked": res["batched"]["tilings_listed"],
+        }), flush=True)
+
+
 FAMILY_TEXT = "aaaaaaaa\naaaaaaaa\naaabaaaa\naaaacaaa\naaaaaaaa\n"
 FAMILY_MAX_STATES = 1 << 30
 
@@ -996,6 +1053,8 @@ def main() -> None:
             bench_serve(args, dist)
         elif args.workload == "family":
             bench_family(args, dist)
+        elif args.workload == "list":
+            bench_list(args, dist)
         else:
             bench_ours(args, dist)
     finally:
