@@ -256,6 +256,7 @@ public:
     // A held instance sits out the following steps (its frontier carried
     // unchanged) while some active instance is not held.
     void set_hold(uint32_t id, bool hold) { inst_.at(id).held = hold; }
+    bool held(uint32_t id) const { return inst_.at(id).held; }
     const std::vector<uint64_t> &level_sizes(uint32_t id) const { return inst_.at(id).level_sizes; }
     uint64_t next_size_estimate(uint32_t id) const;
     // States of the instance's frontier whose current row equals `pattern`.

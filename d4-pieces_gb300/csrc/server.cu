@@ -83,6 +83,12 @@ constexpr uint32_t kSlowChunksPerWarp = 32;
 // many times the cheapest running one's sit out some row steps.
 constexpr double kShareRatio = 8.0;
 
+// A slow-lane row step whose running requests are each projected at no
+// more than this many device bytes (rows of about a million states) does
+// not wait for the fast lane: its kernels are short
+// (D4E_LIGHT_STEP_MB overrides; 0 = every step waits).
+constexpr double kLightStepBytes = 64.0 * (1 << 20);
+
 // Time of the steps without the heavy requests per step with them
 // (D4E_SLOW_SHARE overrides; 0 = no sharing).
 double server_share() {
@@ -170,6 +176,8 @@ public:
             e128.key_mode = KeyMode::K128;
             ln.eng[1] = std::make_unique<Engine>(e128);
         }
+        if (const char *v = std::getenv("D4E_LIGHT_STEP_MB"))
+            light_step_bytes_ = std::atof(v) * (1 << 20);
         if (const char *v = std::getenv("D4E_FAST_STATES"))
             fast_states_ = std::max<uint64_t>(1, std::strtoull(v, nullptr, 10));
         for (int l = 0; l < 2; l++)
@@ -294,17 +302,31 @@ private:
                     std::lock_guard<std::mutex> lk(mu_);
                     st_.lane_admit_ms[l] += ms_between(ta, Clock::now());
                 }
-                if (l == 1 && slow_yield_ms_ > 0) {
-                    // Short requests first: while the fast lane has work, the
-                    // slow lane holds its next row step back (at most
-                    // slow_yield_ms_ per step), so fast-lane rows get the
-                    // whole GPU; heavy requests progress in the gaps.  A step
-                    // that starts with the fast lane idle may be preempted.
-                    std::unique_lock<std::mutex> lk(mu_);
-                    const bool idle = yield_cv_.wait_for(
-                        lk, std::chrono::duration<double, std::milli>(slow_yield_ms_),
-                        [&] { return stop_ || fast_idle(); });
-                    slow_preemptible_ = idle && !stop_;
+                bool held_step[2] = {false, false};
+                if (l == 1) {
+                    bool heavy = false;
+                    for (int e = 0; e < 2; e++) {
+                        if (!ln.eng[e]->has_active())
+                            continue;
+                        held_step[e] = share_ > 0 && plan_share(ln, e);
+                        heavy |= heavy_step(ln, e);
+                    }
+                    if (slow_yield_ms_ > 0) {
+                        // Short requests first: while the fast lane has work,
+                        // the slow lane holds a heavy row step back (at most
+                        // slow_yield_ms_ per step), so fast-lane rows get the
+                        // whole GPU; heavy requests progress in the gaps.  A
+                        // step that starts with the fast lane idle may be
+                        // preempted.
+                        std::unique_lock<std::mutex> lk(mu_);
+                        const auto ready = [&] { return stop_ || fast_idle(); };
+                        const bool idle =
+                            heavy ? yield_cv_.wait_for(
+                                        lk, std::chrono::duration<double, std::milli>(slow_yield_ms_),
+                                        ready)
+                                  : ready();
+                        slow_preemptible_ = idle && !stop_;
+                    }
                 }
                 bool busy = false;
                 for (int e = 0; e < 2; e++) {
@@ -315,7 +337,7 @@ private:
                     const Totals before = ln.eng[e]->totals();
                     const uint64_t restarts0 = before.restarts;
                     const size_t n_run = ln.running[e].size();
-                    const bool held = l == 1 && share_ > 0 && plan_share(ln, e);
+                    const bool held = held_step[e];
                     const StepStats s = ln.eng[e]->step();
                     const auto t1 = Clock::now();
                     if (held) {
@@ -489,6 +511,16 @@ private:
         return lane_[0].n_running + lane_[1].n_running > 1;
     }
 
+    // Whether an engine's next row step runs a request projected above the
+    // light-step bytes (requests sitting the step out do not count).
+    bool heavy_step(Lane &ln, int e) {
+        Engine &eng = *ln.eng[e];
+        for (const auto &[id, r] : ln.running[e])
+            if (!eng.held(id) && (double)eng.projected_bytes(id) > light_step_bytes_)
+                return true;
+        return false;
+    }
+
     // Guarded by mu_.
     bool fast_idle() const { return lane_[0].n_running == 0 && lane_[0].queue.empty(); }
 
@@ -591,6 +623,7 @@ private:
     double slow_yield_ms_ = kSlowYieldMs;
     bool slow_preemptible_ = false;          // guarded by mu_
     double share_ = server_share();          // slow-lane sharing (0: off)
+    double light_step_bytes_ = kLightStepBytes;   // D4E_LIGHT_STEP_MB
     unsigned int *preempt_d_ = nullptr;      // device address of the preemption flag
     uint64_t fast_states_ = kFastStates;   // fast-lane row limit (D4E_FAST_STATES overrides)
     std::deque<d4e_result> results_;
