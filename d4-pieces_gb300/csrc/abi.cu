@@ -518,13 +518,14 @@ void d4e_release_cached_memory(void) { d4e::release_idle_pools(); }
 
 namespace {
 
-// Called for each finished instance of a batch before its engine goes away
-// (engine, engine id, instance index).
-using BatchHook = std::function<void(d4e::Engine &, uint32_t, uint32_t)>;
+// Called once per engine of a batch after it ran, before its results are
+// taken and its instances released: (engine, [(engine id, instance index)]).
+using BatchHook =
+    std::function<void(d4e::Engine &, const std::vector<std::pair<uint32_t, uint32_t>> &)>;
 
 // The batch runner behind d4e_batch_run, d4e_batch_sets and
 // d4e_batch_solutions; `sets` receives each instance's piece multisets in
-// Sets mode, `hook` (list mode) sees each finished instance.
+// Sets mode, `hook` (list mode) sees each engine's finished instances.
 int batch_impl(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts,
                d4e_result *results, d4e_stats *st,
                std::vector<d4e::PieceSets> *sets, const BatchHook &hook = nullptr) {
@@ -547,8 +548,6 @@ int batch_impl(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts
             d4e::engine_result(eng, id, o.mode, &results[i]);
             if (sets && results[i].status == 0)
                 (*sets)[i] = eng.sets(id);
-            if (hook && results[i].status == 0)
-                hook(eng, id, i);
             results[i].tag = i;
             results[i].queued_ms = 0;
             results[i].latency_ms =
@@ -573,6 +572,8 @@ int batch_impl(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts
             for (uint32_t i = 0; i < n; i++) {
                 const uint32_t id = eng.add(to_spec(insts[i], o.mode, o.max_states, o.beam));
                 eng.run();
+                if (hook)
+                    hook(eng, {{id, i}});
                 finish(eng, id, i);
                 eng.release(id);
             }
@@ -602,6 +603,8 @@ int batch_impl(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts
                 }
             }
             eng.run();
+            if (hook)
+                hook(eng, ids);
             for (const auto &[id, i] : ids)
                 finish(eng, id, i);
             if (st)
@@ -615,6 +618,12 @@ int batch_impl(const d4e_instance *insts, uint32_t n, const d4e_batch_opts *opts
             for (uint32_t i : rest)
                 ids.push_back(eng.add(to_spec(insts[i], o.mode, o.max_states, o.beam)));
             eng.run();
+            if (hook) {
+                std::vector<std::pair<uint32_t, uint32_t>> pairs;
+                for (size_t k = 0; k < rest.size(); k++)
+                    pairs.push_back({ids[k], rest[k]});
+                hook(eng, pairs);
+            }
             for (size_t k = 0; k < rest.size(); k++)
                 finish(eng, ids[k], rest[k]);
             if (st)
@@ -683,25 +692,31 @@ int d4e_batch_solutions(const d4e_instance *insts, uint32_t n, const d4e_batch_o
     o.beam = 0;
     if (n && !sol_offsets)
         return fail(D4E_ERR_INVALID, "null pointer");
-    // Each instance's tilings are reconstructed while its engine still holds
-    // its rows, into host buffers of D4E_GRID_CELLS cells per tiling.
+    // The tilings of each engine's instances are reconstructed together
+    // while the engine still holds their rows, into host buffers of
+    // D4E_GRID_CELLS cells per tiling.
     std::vector<std::vector<int8_t>> tg(n);
     std::vector<std::vector<int16_t>> sg(n);
     std::vector<uint64_t> got(n, 0);
-    const BatchHook hook = [&](d4e::Engine &eng, uint32_t id, uint32_t i) {
-        const uint64_t cells = (uint64_t)eng.width(id) * eng.height(id);
-        const uint64_t want = std::min<uint64_t>(max_per_instance, eng.count(id));
-        if (!want)
-            return;
-        std::vector<int8_t> t(want * cells);
-        std::vector<int16_t> sp(want * cells);
-        got[i] = eng.solutions(id, want, t.data(), sp.data(), false);
-        tg[i].assign(got[i] * D4E_GRID_CELLS, -1);
-        sg[i].assign(got[i] * D4E_GRID_CELLS, -1);
-        for (uint64_t k = 0; k < got[i]; k++) {
-            std::memcpy(tg[i].data() + k * D4E_GRID_CELLS, t.data() + k * cells, cells);
-            std::memcpy(sg[i].data() + k * D4E_GRID_CELLS, sp.data() + k * cells,
-                        cells * sizeof(int16_t));
+    const BatchHook hook = [&](d4e::Engine &eng,
+                               const std::vector<std::pair<uint32_t, uint32_t>> &ids) {
+        std::vector<uint32_t> eids;
+        for (const auto &[id, i] : ids)
+            eids.push_back(id);
+        std::vector<d4e::Engine::TilingList> lists;
+        eng.list_solutions(eids, max_per_instance, lists);
+        for (size_t q = 0; q < ids.size(); q++) {
+            const uint32_t id = ids[q].first, i = ids[q].second;
+            const uint64_t cells = (uint64_t)eng.width(id) * eng.height(id);
+            const d4e::Engine::TilingList &l = lists[q];
+            got[i] = l.n;
+            tg[i].assign(l.n * D4E_GRID_CELLS, -1);
+            sg[i].assign(l.n * D4E_GRID_CELLS, -1);
+            for (uint64_t k = 0; k < l.n; k++) {
+                std::memcpy(tg[i].data() + k * D4E_GRID_CELLS, l.types.data() + k * cells, cells);
+                std::memcpy(sg[i].data() + k * D4E_GRID_CELLS, l.steps.data() + k * cells,
+                            cells * sizeof(int16_t));
+            }
         }
     };
     const int rc = batch_impl(insts, n, &o, results, st, nullptr, hook);

@@ -6,6 +6,7 @@
 #include <tuple>
 #include <mutex>
 #include <map>
+#include <memory>
 #include <functional>
 #include <cstdlib>
 #include <cstring>
@@ -2342,6 +2343,323 @@ uint64_t Engine::solutions(uint32_t id, uint64_t max, int8_t *type_grids, int16_
         produced++;
     }
     return produced;
+}
+
+
+void Engine::list_solutions(const std::vector<uint32_t> &ids, uint64_t max_per,
+                            std::vector<TilingList> &out) {
+    EngineScope g(opts_.device, &pool_);
+    out.assign(ids.size(), TilingList{});
+    struct Job {
+        uint32_t id;
+        size_t k;       // index into ids / out
+        uint32_t H;
+        uint64_t cap;   // tilings to list (partial tilings kept per level)
+        std::vector<const ulonglong2 *> lk;   // kept levels
+        std::vector<uint64_t> ln;
+        std::vector<const ulonglong2 *> live; // states of each level on a tiling
+        std::vector<uint64_t> live_n;
+        std::vector<std::vector<PathNode>> nodes;   // partial tilings per level
+    };
+    std::vector<Job> js;
+    for (size_t k = 0; k < ids.size(); k++) {
+        const uint32_t id = ids[k];
+        Inst &in = inst_.at(id);
+        if (in.mode != Mode::List)
+            throw Error(kErrState, "not a list instance");
+        if (!in.done)
+            throw Error(kErrState, "instance has not finished");
+        if (in.status || in.row < in.height || max_per == 0 || count(id) == 0)
+            continue;
+        if (in.levels.size() != (size_t)in.height + 1)
+            throw Error(kErrState, "list level store incomplete");
+        Job j;
+        j.id = id;
+        j.k = k;
+        j.H = in.height;
+        j.cap = std::min<uint64_t>(std::min<uint64_t>(max_per, count(id)), 1u << 26);
+        for (const LevelRef &l : in.levels) {
+            j.lk.push_back(chunks_[l.chunk].keys + l.first);
+            j.ln.push_back(l.len);
+        }
+        j.live.assign(j.H + 1, nullptr);
+        j.live_n.assign(j.H + 1, 0);
+        j.live[j.H] = j.lk[j.H];
+        j.live_n[j.H] = j.ln[j.H];
+        j.nodes.resize(j.H + 1);
+        js.push_back(std::move(j));
+    }
+    if (js.empty())
+        return;
+    uint32_t hmax = 0;
+    for (const Job &j : js)
+        hmax = std::max(hmax, j.H);
+
+    DevBuf<ListJob> djobs;
+    DevBuf<unsigned long long> dcnt;
+    DevBuf<unsigned int> dn;
+    std::vector<std::unique_ptr<DevBuf<ulonglong2>>> owned;   // live-state buffers
+    auto fill_probe = [&](ListJob &lj, const Job &j, uint32_t row) {
+        const Seg sg = seg_for(j.id, row);
+        lj.inst = j.id;
+        lj.row = row;
+        lj.in_shift = sg.in_shift;
+        lj.hi_board = sg.hi_board;
+        lj.tag = sg.tag;
+    };
+    auto upload_jobs = [&](std::vector<ListJob> &v) -> uint32_t {
+        uint32_t b = 0;
+        for (ListJob &lj : v) {
+            lj.blk_base = b;
+            b += list_blocks(lj.n);
+        }
+        djobs.reserve(v.size(), stream_);
+        cuda_check(cudaMemcpyAsync(djobs.p, v.data(), v.size() * sizeof(ListJob),
+                                   cudaMemcpyHostToDevice, stream_),
+                   "upload list jobs");
+        tot_.h2d_bytes += v.size() * sizeof(ListJob);
+        return b;
+    };
+    // Membership set of the given levels' records (all instances in one
+    // table: keys carry their instance); returns its capacity.
+    auto build_set = [&](const std::vector<std::pair<const ulonglong2 *, uint64_t>> &rg) {
+        uint64_t tot = 0;
+        std::vector<ListJob> v;
+        for (const auto &[recs, n] : rg) {
+            tot += n;
+            ListJob lj{};
+            lj.recs = recs;
+            lj.n = n;
+            v.push_back(lj);
+        }
+        uint64_t cap = round_up(std::max<uint64_t>(tot * 2, 1024), 1024);
+        for (;;) {
+            const uint64_t units = cap * slot_units();
+            if (table_.cap < units) {
+                table_.release();
+                table_clean_ = 0;
+                table_.reserve(units, stream_);
+            }
+            cuda_check(cudaMemsetAsync(table_.p, 0, units * sizeof(ulonglong2), stream_),
+                       "memset");
+            cuda_check(cudaMemsetAsync(misc_.p, 0, sizeof(unsigned int), stream_), "memset");
+            const uint32_t blocks = upload_jobs(v);
+            KeySetArgs t{table_.p, cap, misc_.p, opts_.max_probe};
+            launch_keyset_insert_jobs(k64_, t, djobs.p, (uint32_t)v.size(), blocks, stream_);
+            cuda_check(cudaGetLastError(), "k_keyset_insert_jobs launch");
+            tot_.other_launches++;
+            unsigned int stt = 0;
+            cuda_check(cudaMemcpyAsync(&stt, misc_.p, sizeof(unsigned int),
+                                       cudaMemcpyDeviceToHost, stream_),
+                       "read status");
+            cuda_check(cudaStreamSynchronize(stream_), "k_keyset_insert_jobs");
+            if (!(stt & kStatusTableOverflow))
+                return cap;
+            cap *= 4;
+        }
+    };
+    auto probe_base = [&](uint64_t cap) {
+        ProbeArgs p{};
+        p.insts = insts_.p;
+        p.plc = plc_.p;
+        p.table = table_.p;
+        p.cap = cap;
+        p.max_probe = opts_.max_probe;
+        return p;
+    };
+
+    // Backward pass, aligned at the instances' last rows: step t marks level
+    // H - 1 - t of every instance taller than t, keeping the states with a
+    // child among the next level's live states.
+    for (uint32_t t = 0; t < hmax; t++) {
+        std::vector<size_t> act;
+        std::vector<std::pair<const ulonglong2 *, uint64_t>> rg;
+        for (size_t q = 0; q < js.size(); q++)
+            if (js[q].H > t) {
+                act.push_back(q);
+                const uint32_t r = js[q].H - 1 - t;
+                rg.push_back({js[q].live[r + 1], js[q].live_n[r + 1]});
+            }
+        const uint64_t cap = build_set(rg);
+        std::vector<ListJob> v;
+        uint64_t off = 0;
+        for (size_t q : act) {
+            const Job &j = js[q];
+            const uint32_t r = j.H - 1 - t;
+            ListJob lj{};
+            lj.recs = j.lk[r];
+            lj.n = j.ln[r];
+            lj.out_off = off;
+            lj.out_cap = j.ln[r];
+            fill_probe(lj, j, r);
+            off += j.ln[r];
+            v.push_back(lj);
+        }
+        owned.push_back(std::make_unique<DevBuf<ulonglong2>>());
+        DevBuf<ulonglong2> &dst = *owned.back();
+        dst.reserve(std::max<uint64_t>(off, 1), stream_);
+        dcnt.reserve(act.size(), stream_);
+        cuda_check(cudaMemsetAsync(dcnt.p, 0, act.size() * sizeof(unsigned long long), stream_),
+                   "memset");
+        const uint32_t blocks = upload_jobs(v);
+        launch_mark_select_jobs(k64_, probe_base(cap), djobs.p, (uint32_t)v.size(), blocks, dst.p,
+                                dcnt.p, stream_);
+        cuda_check(cudaGetLastError(), "k_mark_select_jobs launch");
+        tot_.other_launches++;
+        std::vector<unsigned long long> cn(act.size());
+        cuda_check(cudaMemcpyAsync(cn.data(), dcnt.p, cn.size() * sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, stream_),
+                   "read live counts");
+        cuda_check(cudaStreamSynchronize(stream_), "k_mark_select_jobs");
+        for (size_t a = 0; a < act.size(); a++) {
+            Job &j = js[act[a]];
+            const uint32_t r = j.H - 1 - t;
+            j.live[r] = dst.p + v[a].out_off;
+            j.live_n[r] = cn[a];
+        }
+    }
+
+    // Forward pass, aligned at the first row: partial tilings of every
+    // instance taller than r extended by one row through live states.
+    DevBuf<PathNode> din, dout;
+    {
+        std::vector<PathNode> roots(js.size());
+        for (size_t q = 0; q < js.size(); q++) {
+            ulonglong2 rk;
+            cuda_check(cudaMemcpyAsync(&rk, js[q].lk[0], sizeof(rk), cudaMemcpyDeviceToHost,
+                                       stream_),
+                       "read root");
+            cuda_check(cudaStreamSynchronize(stream_), "read root");
+            PathNode &nd = roots[q];
+            nd = PathNode{};
+            nd.k0 = rk.x;
+            nd.k1 = k64_ ? 0ull : rk.y;
+            nd.parent = ~0u;
+            nd.nfill = 0;
+            js[q].nodes[0].push_back(nd);
+        }
+        din.reserve(roots.size(), stream_);
+        cuda_check(cudaMemcpyAsync(din.p, roots.data(), roots.size() * sizeof(PathNode),
+                                   cudaMemcpyHostToDevice, stream_),
+                   "upload roots");
+        cuda_check(cudaStreamSynchronize(stream_), "upload roots");
+    }
+    // Node offsets of each instance in din (level r).
+    std::vector<uint64_t> in_off(js.size());
+    for (size_t q = 0; q < js.size(); q++)
+        in_off[q] = q;
+    for (uint32_t r = 0; r < hmax; r++) {
+        std::vector<size_t> act;
+        std::vector<std::pair<const ulonglong2 *, uint64_t>> rg;
+        for (size_t q = 0; q < js.size(); q++)
+            if (js[q].H > r && !js[q].nodes[r].empty()) {
+                act.push_back(q);
+                rg.push_back({js[q].live[r + 1], js[q].live_n[r + 1]});
+            }
+        if (act.empty())
+            break;
+        const uint64_t cap = build_set(rg);
+        std::vector<ListJob> v;
+        uint64_t off = 0;
+        for (size_t q : act) {
+            const Job &j = js[q];
+            ListJob lj{};
+            lj.nodes = din.p + in_off[q];
+            lj.n = j.nodes[r].size();
+            lj.out_off = off;
+            lj.out_cap = j.cap;
+            fill_probe(lj, j, r);
+            off += j.cap;
+            v.push_back(lj);
+        }
+        dout.reserve(std::max<uint64_t>(off, 1), stream_);
+        dn.reserve(act.size(), stream_);
+        cuda_check(cudaMemsetAsync(dn.p, 0, act.size() * sizeof(unsigned int), stream_), "memset");
+        cuda_check(cudaMemsetAsync(misc_.p, 0, sizeof(unsigned int), stream_), "memset");
+        const uint32_t blocks = upload_jobs(v);
+        launch_extend_paths_jobs(k64_, probe_base(cap), djobs.p, (uint32_t)v.size(), blocks,
+                                 dout.p, dn.p, misc_.p, stream_);
+        cuda_check(cudaGetLastError(), "k_extend_paths_jobs launch");
+        tot_.other_launches++;
+        std::vector<unsigned int> cn(act.size());
+        cuda_check(cudaMemcpyAsync(cn.data(), dn.p, cn.size() * sizeof(unsigned int),
+                                   cudaMemcpyDeviceToHost, stream_),
+                   "read nodes");
+        cuda_check(cudaStreamSynchronize(stream_), "k_extend_paths_jobs");
+        // The new partial tilings: one read of the whole output when it is
+        // small, else each instance's part.
+        const bool bulk = off * sizeof(PathNode) <= (64ull << 20);
+        std::vector<PathNode> host(bulk ? off : 0);
+        if (bulk) {
+            cuda_check(cudaMemcpyAsync(host.data(), dout.p, off * sizeof(PathNode),
+                                       cudaMemcpyDeviceToHost, stream_),
+                       "read nodes");
+            tot_.d2h_bytes += off * sizeof(PathNode);
+        }
+        for (size_t a = 0; a < act.size(); a++) {
+            Job &j = js[act[a]];
+            const uint64_t got = std::min<uint64_t>(cn[a], j.cap);
+            j.nodes[r + 1].resize(got);
+            if (!bulk && got) {
+                cuda_check(cudaMemcpyAsync(j.nodes[r + 1].data(), dout.p + v[a].out_off,
+                                           got * sizeof(PathNode), cudaMemcpyDeviceToHost,
+                                           stream_),
+                           "read nodes");
+                tot_.d2h_bytes += got * sizeof(PathNode);
+            }
+            in_off[act[a]] = v[a].out_off;
+        }
+        cuda_check(cudaStreamSynchronize(stream_), "read nodes");
+        if (bulk)
+            for (size_t a = 0; a < act.size(); a++) {
+                Job &j = js[act[a]];
+                std::copy(host.begin() + (std::ptrdiff_t)v[a].out_off,
+                          host.begin() + (std::ptrdiff_t)(v[a].out_off + j.nodes[r + 1].size()),
+                          j.nodes[r + 1].begin());
+            }
+        std::swap(din.p, dout.p);
+        std::swap(din.cap, dout.cap);
+        std::swap(din.s, dout.s);
+    }
+    owned.clear();
+    table_clean_ = 0;   // the table now holds membership sets
+
+    // Leaves -> grids, as solutions() writes them.
+    for (Job &j : js) {
+        const Inst &in = inst_[j.id];
+        const uint32_t W = in.width, H = j.H, cells = W * H;
+        const auto &lib = in.lib;
+        TilingList &tl = out[j.k];
+        const auto &leaves = j.nodes[H];
+        const uint64_t n = std::min<uint64_t>(leaves.size(), j.cap);
+        tl.n = n;
+        tl.types.assign(n * cells, -1);
+        tl.steps.assign(n * cells, -1);
+        for (uint64_t q = 0; q < n; q++) {
+            std::vector<const PathNode *> chain(H);
+            const PathNode *nd = &leaves[q];
+            for (int r = (int)H; r >= 1; r--) {
+                chain[r - 1] = nd;
+                nd = r >= 2 ? &j.nodes[r - 1][nd->parent] : nullptr;
+            }
+            int8_t *tg = tl.types.data() + q * cells;
+            int16_t *sg = tl.steps.data() + q * cells;
+            int step = 0;
+            for (uint32_t r = 0; r < H; r++) {
+                const PathNode *pn = chain[r];
+                for (uint32_t d = 0; d < pn->nfill; d++, step++) {
+                    const uint32_t pi = pn->plc[d];
+                    for (uint64_t bits = lib.plc[pi].mask; bits; bits &= bits - 1) {
+                        const uint32_t cell = r * W + (uint32_t)__builtin_ctzll(bits);
+                        if (cell < cells) {
+                            tg[cell] = (int8_t)lib.plc_type[pi];
+                            sg[cell] = (int16_t)step;
+                        }
+                    }
+                }
+            }
+        }
+    }
 }
 
 }  // namespace d4e

@@ -271,6 +271,17 @@ public:
     // count unless max truncated it).
     uint64_t solutions(uint32_t id, uint64_t max, int8_t *type_grids, int16_t *step_grids,
                        bool single);
+    // Tilings of many finished Mode::List instances at once, at most max_per
+    // each: the backward (live-state) and forward (path) passes cover every
+    // instance per level, one launch per level and pass.  out[k] receives
+    // ids[k]'s tilings (none for a failed instance or one without tilings).
+    struct TilingList {
+        uint64_t n = 0;                  // tilings written
+        std::vector<int8_t> types;       // n grids of width * height cells
+        std::vector<int16_t> steps;
+    };
+    void list_solutions(const std::vector<uint32_t> &ids, uint64_t max_per,
+                        std::vector<TilingList> &out);
 
     const Totals &totals() const { return tot_; }
     const Tuning &tuning() const { return tune_; }

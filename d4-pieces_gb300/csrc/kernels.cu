@@ -1292,6 +1292,147 @@ k_extend_paths(ProbeArgs p, const PathNode *__restrict__ nodes, uint32_t n_nodes
     }
 }
 
+// ---- listing over many instances: jobs dealt to blocks -----------------
+// The job of block b: the last job whose blk_base <= b.
+__device__ __forceinline__ uint32_t list_job_of(const ListJob *jobs, uint32_t n_jobs, uint32_t b) {
+    uint32_t lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].blk_base <= b)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// The job's blocks: from its blk_base to the next job's (the last job runs
+// to the grid's end).
+__device__ __forceinline__ uint32_t list_job_blocks(const ListJob *jobs, uint32_t n_jobs,
+                                                    uint32_t j) {
+    return (j + 1 < n_jobs ? jobs[j + 1].blk_base : gridDim.x) - jobs[j].blk_base;
+}
+
+__device__ __forceinline__ ProbeArgs list_probe(const ProbeArgs &base, const ListJob &jb) {
+    ProbeArgs p = base;
+    p.inst = jb.inst;
+    p.row = jb.row;
+    p.in_shift = jb.in_shift;
+    p.hi_board = jb.hi_board;
+    p.tag = jb.tag;
+    return p;
+}
+
+template <bool K64>
+__global__ void k_keyset_insert_jobs(KeySetArgs t, const ListJob *__restrict__ jobs,
+                                     uint32_t n_jobs) {
+    const uint32_t j = list_job_of(jobs, n_jobs, blockIdx.x);
+    const ListJob jb = jobs[j];
+    const unsigned long long stride =
+        (unsigned long long)list_job_blocks(jobs, n_jobs, j) * blockDim.x;
+    for (unsigned long long i = (unsigned long long)(blockIdx.x - jb.blk_base) * blockDim.x +
+                                threadIdx.x;
+         i < jb.n; i += stride) {
+        const ulonglong2 k = jb.recs[i];
+        int r;
+        if constexpr (K64)
+            r = insert64(static_cast<Slot16 *>(t.table), t.cap, k.x, 0ull, t.max_probe);
+        else
+            r = insert128(static_cast<Slot32 *>(t.table), t.cap, k.x, k.y, 0ull, t.max_probe);
+        if (r < 0)
+            atomicOr(t.status, kStatusTableOverflow);
+    }
+}
+
+template <bool K64>
+__global__ void __launch_bounds__(kExpandBlock)
+k_mark_select_jobs(ProbeArgs base, const ListJob *__restrict__ jobs, uint32_t n_jobs,
+                   ulonglong2 *__restrict__ out, unsigned long long *__restrict__ n_out) {
+    __shared__ SmemTable st;
+    const uint32_t j = list_job_of(jobs, n_jobs, blockIdx.x);
+    const ListJob jb = jobs[j];
+    const ProbeArgs p = list_probe(base, jb);
+    load_table(st, p.insts + p.inst, p.plc);
+    __syncthreads();
+    const Codec cd = make_codec(st, p.hi_board, p.in_shift, p.tag);
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned long long stride =
+        (unsigned long long)list_job_blocks(jobs, n_jobs, j) * blockDim.x;
+    // Warp-uniform trip count: every lane takes part in the ballot.
+    for (unsigned long long base_i = (unsigned long long)(blockIdx.x - jb.blk_base) * blockDim.x;
+         base_i < jb.n; base_i += stride) {
+        const unsigned long long i = base_i + threadIdx.x;
+        bool keep = false;
+        ulonglong2 k = make_ulonglong2(0ull, 0ull);
+        if (i < jb.n) {
+            k = jb.recs[i];
+            unsigned long long w, u;
+            parse_key<K64>(cd, k.x, k.y, w, u);
+            row_fills(st, w, u,
+                      [&](unsigned long long wd, unsigned long long ud, unsigned long long,
+                          uint32_t, uint32_t) {
+                          unsigned long long a, b;
+                          keep = probe_child<K64>(p, cd, wd, ud, a, b);
+                          return keep;
+                      });
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        unsigned long long b = 0;
+        if (lane == 0 && m)
+            b = atomicAdd(n_out + j, (unsigned long long)__popc(m));
+        b = __shfl_sync(0xffffffffu, b, 0);
+        if (keep)
+            out[jb.out_off + b + __popc(m & ((1u << lane) - 1u))] = k;
+    }
+}
+
+template <bool K64>
+__global__ void __launch_bounds__(kExpandBlock)
+k_extend_paths_jobs(ProbeArgs base, const ListJob *__restrict__ jobs, uint32_t n_jobs,
+                    PathNode *__restrict__ out, unsigned int *__restrict__ n_out,
+                    unsigned int *__restrict__ status) {
+    __shared__ SmemTable st;
+    const uint32_t j = list_job_of(jobs, n_jobs, blockIdx.x);
+    const ListJob jb = jobs[j];
+    const ProbeArgs p = list_probe(base, jb);
+    load_table(st, p.insts + p.inst, p.plc);
+    __syncthreads();
+    const Codec cd = make_codec(st, p.hi_board, p.in_shift, p.tag);
+    const unsigned long long stride =
+        (unsigned long long)list_job_blocks(jobs, n_jobs, j) * blockDim.x;
+    for (unsigned long long i = (unsigned long long)(blockIdx.x - jb.blk_base) * blockDim.x +
+                                threadIdx.x;
+         i < jb.n; i += stride) {
+        const PathNode nd = jb.nodes[i];
+        unsigned long long w, u;
+        parse_key<K64>(cd, nd.k0, nd.k1, w, u);
+        row_fills(st, w, u,
+                  [&](unsigned long long wd, unsigned long long ud, unsigned long long sidx,
+                      uint32_t scol, uint32_t depth) {
+                      unsigned long long ck0, ck1;
+                      if (!probe_child<K64>(p, cd, wd, ud, ck0, ck1))
+                          return false;
+                      const unsigned pos = atomicAdd(n_out + j, 1u);
+                      if (pos >= jb.out_cap) {
+                          atomicOr(status, kStatusNodeOverflow);
+                          return true;
+                      }
+                      PathNode o;
+                      o.k0 = ck0;
+                      o.k1 = ck1;
+                      o.parent = (uint32_t)i;
+                      o.nfill = depth;
+                      for (uint32_t d = 0; d < (uint32_t)kMaxWidth; d++) {
+                          const uint32_t c = (scol >> (4 * d)) & 0xFu;
+                          const uint32_t ix = (uint32_t)(sidx >> (8 * d)) & 0xFFu;
+                          o.plc[d] = d < depth ? (uint16_t)(st.off[c] + ix) : (uint16_t)0xFFFFu;
+                      }
+                      out[jb.out_off + pos] = o;
+                      return false;
+                  });
+    }
+}
+
 // Partitioned dedup, second half: one bucket per block iteration.
 constexpr int kMergeBlock = 512;
 constexpr unsigned kMergeProbe = 256;
@@ -1504,6 +1645,45 @@ void launch_extend_paths(bool k64, const ProbeArgs &p, const PathNode *nodes, ui
     else
         k_extend_paths<false><<<grid, kExpandBlock, 0, s>>>(p, nodes, n_nodes, out, n_out,
                                                             max_out, status);
+}
+
+uint32_t list_blocks(unsigned long long n) {
+    const unsigned long long b = (n + kExpandBlock - 1) / kExpandBlock;
+    return (uint32_t)std::min<unsigned long long>(std::max<unsigned long long>(b, 1), kListMaxBlocks);
+}
+
+void launch_keyset_insert_jobs(bool k64, const KeySetArgs &t, const ListJob *jobs,
+                               uint32_t n_jobs, uint32_t blocks, cudaStream_t s) {
+    if (n_jobs == 0 || blocks == 0)
+        return;
+    if (k64)
+        k_keyset_insert_jobs<true><<<blocks, kExpandBlock, 0, s>>>(t, jobs, n_jobs);
+    else
+        k_keyset_insert_jobs<false><<<blocks, kExpandBlock, 0, s>>>(t, jobs, n_jobs);
+}
+
+void launch_mark_select_jobs(bool k64, const ProbeArgs &p, const ListJob *jobs, uint32_t n_jobs,
+                             uint32_t blocks, ulonglong2 *out, unsigned long long *n_out,
+                             cudaStream_t s) {
+    if (n_jobs == 0 || blocks == 0)
+        return;
+    if (k64)
+        k_mark_select_jobs<true><<<blocks, kExpandBlock, 0, s>>>(p, jobs, n_jobs, out, n_out);
+    else
+        k_mark_select_jobs<false><<<blocks, kExpandBlock, 0, s>>>(p, jobs, n_jobs, out, n_out);
+}
+
+void launch_extend_paths_jobs(bool k64, const ProbeArgs &p, const ListJob *jobs, uint32_t n_jobs,
+                              uint32_t blocks, PathNode *out, unsigned int *n_out,
+                              unsigned int *status, cudaStream_t s) {
+    if (n_jobs == 0 || blocks == 0)
+        return;
+    if (k64)
+        k_extend_paths_jobs<true><<<blocks, kExpandBlock, 0, s>>>(p, jobs, n_jobs, out, n_out,
+                                                                  status);
+    else
+        k_extend_paths_jobs<false><<<blocks, kExpandBlock, 0, s>>>(p, jobs, n_jobs, out, n_out,
+                                                                   status);
 }
 
 void launch_select(const ulonglong2 *recs, const unsigned char *alive, unsigned long long n,

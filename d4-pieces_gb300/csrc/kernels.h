@@ -163,6 +163,46 @@ void launch_extend_paths(bool k64, const ProbeArgs &p, const PathNode *nodes, ui
 void launch_select(const ulonglong2 *recs, const unsigned char *alive, unsigned long long n,
                    ulonglong2 *out, unsigned long long *n_out, int grid, cudaStream_t s);
 
+// Solution listing over many instances at once: one job per instance and
+// level, each launch covering every job (blocks are dealt to jobs by
+// blk_base; a block works on one job and loads that instance's placement
+// table).  The membership set holds the live states of every job's next
+// level together: keys carry their instance.
+struct ListJob {
+    const ulonglong2 *recs;         // the job's level records (keyset / mark passes)
+    const PathNode *nodes;          // the job's partial tilings (extend pass)
+    unsigned long long n;           // records or nodes
+    unsigned long long out_off;     // the job's region of the output buffer
+    unsigned long long out_cap;     // its size (extend pass: nodes kept)
+    unsigned long long in_shift, hi_board, tag;   // probe fields of the job's row
+    uint32_t inst, row;
+    uint32_t blk_base;              // first block of the job (jobs in block order)
+    uint32_t pad;
+};
+
+// Blocks for a job of n items (at least one, at most kListMaxBlocks).
+constexpr uint32_t kListMaxBlocks = 64;
+uint32_t list_blocks(unsigned long long n);
+
+// Insert every job's records into the membership set.
+void launch_keyset_insert_jobs(bool k64, const KeySetArgs &t, const ListJob *jobs,
+                               uint32_t n_jobs, uint32_t blocks, cudaStream_t s);
+
+// Every job's records with a child in the set, appended to out + out_off
+// (n_out[job] counts them; order not preserved).  p: instance tables and
+// the set (per-job fields are taken from the jobs).
+void launch_mark_select_jobs(bool k64, const ProbeArgs &p, const ListJob *jobs, uint32_t n_jobs,
+                             uint32_t blocks, ulonglong2 *out, unsigned long long *n_out,
+                             cudaStream_t s);
+
+// For every job's nodes, one PathNode per (row fill, child in the set), at
+// out + out_off + position (n_out[job] counts them; positions at or past
+// out_cap are dropped and flag kStatusNodeOverflow).  parent = the node's
+// index within its job.
+void launch_extend_paths_jobs(bool k64, const ProbeArgs &p, const ListJob *jobs, uint32_t n_jobs,
+                              uint32_t blocks, PathNode *out, unsigned int *n_out,
+                              unsigned int *status, cudaStream_t s);
+
 // *out += number of records with (rec.x & mask) == value.
 void launch_count_pattern(const ulonglong2 *recs, unsigned long long n, unsigned long long mask,
                           unsigned long long value, unsigned long long *out, int grid,
