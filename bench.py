@@ -527,6 +527,7 @@ def bench_ours(args, dist: Dist) -> None:
                                           args.mix_max_states, MIX_BEAM, SERVE_GRACE)
         line["served_light"] = serve_section(E, dev, SERVE_LIGHT_RATE, args.serve_light_seconds,
                                              args.mix_max_states, MIX_BEAM, SERVE_GRACE)
+        line["batched_list"] = list_section(E, dev, LIST_INSTANCES)
     print(json.dumps(line), flush=True)
 
 
@@ -642,25 +643,24 @@ def bench_batched(args, dist: Dist) -> None:
 
 LIST_MAX_CELLS = 40
 LIST_PER_INSTANCE = 64
+LIST_INSTANCES = 1024
 
 
-def bench_list(args, dist: Dist) -> None:
+def list_section(E, dev: int, n: int) -> dict:
     """Batched solution listing: the tilings of the batched mix's boards of
     at most LIST_MAX_CELLS cells (up to LIST_PER_INSTANCE per board), once
     as one batch (d4e_batch_solutions) and once one board at a time through
     the same call.  Counts must agree; boards with at most
     LIST_PER_INSTANCE tilings must list the same tilings in both arms; every
     listed tiling passes the independent cover check."""
-    from d4gb import engine as E
     from d4gb.problem import batched_mix, verify_tiling
 
-    probs = [p for p in batched_mix(BATCHED_SEED, 16 * args.instances)
-             if p.cells <= LIST_MAX_CELLS][: args.instances]
+    probs = [p for p in batched_mix(BATCHED_SEED, 16 * n) if p.cells <= LIST_MAX_CELLS][:n]
     res, outs = {}, {}
     for arm, seq in (("batched", False), ("plain", True)):
         t0 = time.perf_counter()
         grids, out, st = E.batch_solutions(probs, max_per_instance=LIST_PER_INSTANCE,
-                                           device=dist.local_rank, sequential=seq)
+                                           device=dev, sequential=seq)
         wall = time.perf_counter() - t0
         outs[arm] = (grids, out)
         listed = sum(len(g[0]) for g in grids)
@@ -680,20 +680,29 @@ def bench_list(args, dist: Dist) -> None:
         for t, s_ in zip(*gb[i]):
             if not verify_tiling(p, t, s_):
                 raise RuntimeError(f"board {i}: a listed tiling fails the cover check")
-    if dist.rank == 0:
-        print(json.dumps({
-            "metric": "puzzles/s (batched solution listing)",
-            "value": res["batched"]["puzzles_per_s"],
-            "unit": "puzzles/s",
-            "n_gpus": dist.world,
-            "config": {"workload": f"batched mix boards of at most {LIST_MAX_CELLS} cells: "
-                                   f"{len(probs)} boards, seed {BATCHED_SEED}, up to "
-                                   f"{LIST_PER_INSTANCE} tilings listed per board"},
+    return {"workload": f"batched mix boards of at most {LIST_MAX_CELLS} cells: "
+                        f"{len(probs)} boards, seed {BATCHED_SEED}, up to "
+                        f"{LIST_PER_INSTANCE} tilings listed per board",
             "boards_with_tilings": sum(1 for r in ob if r["count"]),
             "tilings_total": sum(r["count"] for r in ob),
             "batched": res["batched"], "plain": res["plain"],
             "speedup_vs_plain": res["batched"]["puzzles_per_s"] / res["plain"]["puzzles_per_s"],
-            "cover_checked": res["batched"]["tilings_listed"],
+            "cover_checked": res["batched"]["tilings_listed"]}
+
+
+def bench_list(args, dist: Dist) -> None:
+    """The batched listing section alone (--instances boards)."""
+    from d4gb import engine as E
+
+    sec = list_section(E, dist.local_rank, args.instances)
+    if dist.rank == 0:
+        print(json.dumps({
+            "metric": "puzzles/s (batched solution listing)",
+            "value": sec["batched"]["puzzles_per_s"],
+            "unit": "puzzles/s",
+            "n_gpus": dist.world,
+            "config": {"workload": sec.pop("workload")},
+            **sec,
         }), flush=True)
 
 
