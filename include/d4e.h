@@ -338,7 +338,11 @@ int d4e_batch_solutions(const d4e_instance *insts, uint32_t n, const d4e_batch_o
  * different times shares each k_expand / k_compact launch.  Two lanes run
  * concurrently on their own streams: every request starts in the fast lane
  * (rows of at most 2^17 distinct states); one that outgrows it restarts in
- * the slow lane, whose kernels leave room on every SM for the fast lane's.
+ * the slow lane, whose kernels leave room on every SM for the fast lane's,
+ * whose heavy row steps wait for (and whose k_expand launches are preempted
+ * by) fast-lane work, and whose heaviest requests sit out some row steps so
+ * that lighter ones are not paced by them.  A request that runs out of
+ * device memory beside others restarts in the slow lane (at most twice).
  * Results are the same as alone (counts exact; solve-one tilings as in
  * d4e_batch_run).
  * ---------------------------------------------------------------------- */
