@@ -267,9 +267,9 @@ private:
         double projected = 0;                                 // guarded by mu_
         double avg_peak = 0;                                  // worker-owned
         uint64_t n_peaks = 0;
-        // Slow-lane sharing, per engine: time of the last step that ran
-        // every request, and of the steps without the heavy ones since.
-        double last_full_ms[2] = {0, 0}, owed_ms[2] = {0, 0};
+        // Slow-lane sharing: time of the last row step that ran every
+        // request, and of the steps without the heavy ones since.
+        double last_full_ms = 0, owed_ms = 0;
     };
 
     // Bytes charged for a request not yet started: solve-one requests are
@@ -302,15 +302,15 @@ private:
                     std::lock_guard<std::mutex> lk(mu_);
                     st_.lane_admit_ms[l] += ms_between(ta, Clock::now());
                 }
-                bool held_step[2] = {false, false};
+                bool sit_out[2] = {false, false};   // engine whose every request sits out
+                bool held_any = false;
                 if (l == 1) {
+                    if (share_ > 0)
+                        held_any = plan_share(ln, sit_out);
                     bool heavy = false;
-                    for (int e = 0; e < 2; e++) {
-                        if (!ln.eng[e]->has_active())
-                            continue;
-                        held_step[e] = share_ > 0 && plan_share(ln, e);
-                        heavy |= heavy_step(ln, e);
-                    }
+                    for (int e = 0; e < 2; e++)
+                        if (ln.eng[e]->has_active() && !sit_out[e])
+                            heavy |= heavy_step(ln, e);
                     if (slow_yield_ms_ > 0) {
                         // Short requests first: while the fast lane has work,
                         // the slow lane holds a heavy row step back (at most
@@ -329,23 +329,20 @@ private:
                     }
                 }
                 bool busy = false;
+                double step_ms = 0;
                 for (int e = 0; e < 2; e++) {
                     if (!ln.eng[e]->has_active())
                         continue;
                     busy = true;
+                    if (sit_out[e])
+                        continue;
                     const auto t0 = Clock::now();
                     const Totals before = ln.eng[e]->totals();
                     const uint64_t restarts0 = before.restarts;
                     const size_t n_run = ln.running[e].size();
-                    const bool held = held_step[e];
                     const StepStats s = ln.eng[e]->step();
                     const auto t1 = Clock::now();
-                    if (held) {
-                        ln.owed_ms[e] += ms_between(t0, t1);
-                    } else if (l == 1) {
-                        ln.last_full_ms[e] = ms_between(t0, t1);
-                        ln.owed_ms[e] = 0;
-                    }
+                    step_ms += ms_between(t0, t1);
                     collect(l, e);
                     const auto t2 = Clock::now();
                     const Totals &after = ln.eng[e]->totals();
@@ -371,6 +368,14 @@ private:
                     st_.restarts += ln.eng[e]->totals().restarts - restarts0;
                     st_.preemptions += after.preemptions - before.preemptions;
                     st_.paused += s.paused;
+                }
+                if (l == 1 && busy) {
+                    if (held_any) {
+                        ln.owed_ms += step_ms;
+                    } else {
+                        ln.last_full_ms = step_ms;
+                        ln.owed_ms = 0;
+                    }
                 }
                 if (l == 0)
                     yield_cv_.notify_all();
@@ -481,26 +486,35 @@ private:
         }
     }
 
-    // Sharing in the slow lane: one row step advances every running request,
-    // and requests that outgrew the fast lane differ in row cost by orders of
-    // magnitude.  While some running requests' next rows are projected at
-    // more than kShareRatio times the cheapest one's, those heavy ones sit
-    // out row steps until the steps without them have taken as long as the
-    // last step with them: the others move at their own pace, and the heavy
-    // ones keep about half of the lane's time.  Returns whether any request
-    // sits out the next step.
-    bool plan_share(Lane &ln, int e) {
-        Engine &eng = *ln.eng[e];
+    // Sharing in the slow lane: one row step advances every running request
+    // of both engines (one after the other), and requests that outgrew the
+    // fast lane differ in row cost by orders of magnitude.  While some
+    // running requests' next rows are projected at more than kShareRatio
+    // times the cheapest one's (over both engines), those heavy ones sit out
+    // row steps until the steps without them have taken as long as the last
+    // step with them: the others move at their own pace, and the heavy ones
+    // keep about half of the lane's time.  An engine whose every request
+    // sits out is not stepped (sit_out).  Returns whether any request sits
+    // out the next step.
+    bool plan_share(Lane &ln, bool sit_out[2]) {
         uint64_t cheapest = UINT64_MAX;
-        for (const auto &[id, r] : ln.running[e])
-            cheapest = std::min<uint64_t>(cheapest, std::max<uint64_t>(eng.projected_bytes(id), 1));
-        const bool light_turn = ln.owed_ms[e] < share_ * ln.last_full_ms[e];
+        for (int e = 0; e < 2; e++)
+            for (const auto &[id, r] : ln.running[e])
+                cheapest = std::min<uint64_t>(
+                    cheapest, std::max<uint64_t>(ln.eng[e]->projected_bytes(id), 1));
+        const bool light_turn = ln.owed_ms < share_ * ln.last_full_ms;
         bool any = false;
-        for (const auto &[id, r] : ln.running[e]) {
-            const bool hold = light_turn && (double)eng.projected_bytes(id) >
-                                                kShareRatio * (double)cheapest;
-            eng.set_hold(id, hold);
-            any |= hold;
+        for (int e = 0; e < 2; e++) {
+            Engine &eng = *ln.eng[e];
+            bool all = !ln.running[e].empty();
+            for (const auto &[id, r] : ln.running[e]) {
+                const bool hold = light_turn && (double)eng.projected_bytes(id) >
+                                                    kShareRatio * (double)cheapest;
+                eng.set_hold(id, hold);
+                any |= hold;
+                all &= hold;
+            }
+            sit_out[e] = all;
         }
         return any;
     }
