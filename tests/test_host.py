@@ -165,3 +165,14 @@ def test_cpp_facade_builds_and_fails_like_reference_without_gpu(engine):
         pytest.skip("a GPU is present")
     r = subprocess.run([str(exe), "0xFFFFFFE7E7FFFFFF", "5", "5"], capture_output=True, text=True)
     assert r.returncode == 1 and "no CUDA device" in r.stderr
+
+
+def test_list_mode_runs_only_through_batch_solutions(engine):
+    """D4E_MODE_LIST keeps every row on the device for the listing call;
+    d4e_batch_run refuses it (argument check, before any device work)."""
+    from d4gb.problem import Problem
+
+    p = Problem(4, 2, [0xF, 0xF], [0x3], [4], 0xFF)
+    with pytest.raises(engine.D4Error) as e:
+        engine.batch_run([p], mode=engine.MODE_LIST)
+    assert e.value.code == -1 and "d4e_batch_solutions" in str(e.value)
