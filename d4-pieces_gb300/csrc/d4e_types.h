@@ -102,9 +102,13 @@ constexpr uint32_t kInstWitness = 1u;
 struct Seg {
     uint32_t inst;
     uint32_t row;                 // row being completed
-    uint64_t begin;
-    uint64_t len;
+    uint64_t begin;               // first work item (items of all segments are consecutive)
+    uint64_t len;                 // work items: states x items per state
     uint64_t chunk_base;
+    uint64_t rec;                 // the segment's first frontier record
+    // Work items per state: 1 (levels 0), or the state's walk cut by its
+    // first placement (levels 1: fan items) or first two (levels 2: fan^2).
+    uint32_t fan, levels;
     unsigned long long in_shift;  // K128: board row (row + R) entering window row R-1
     unsigned long long hi_board;  // K64: board rows [row + dyn_rows, row + R) in window coordinates
     unsigned long long tag;       // instance id bits | marker, in the mode's key coordinates

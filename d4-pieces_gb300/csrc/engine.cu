@@ -878,17 +878,39 @@ StepStats Engine::step_impl() {
         // must not flood the GPU with mostly empty items.  Larger frontiers
         // already fill the GPU, and warps fetch chunks independently with
         // in-warp work donation.
-        uint32_t fan = 0;
-        if (n_grp * 4 < slots * 256)
-            for (uint32_t id : grp)
+        // The split is chosen per instance (Seg::levels): in a large group
+        // (a batch), an instance whose states each expect far more children
+        // than a lane's share of the launch -- a first row, or a few states
+        // of a wide board -- is split too, so that its walks do not keep a
+        // handful of lanes busy long after the rest of the GPU has finished.
+        // fan = the instance's longest placement list of a column.
+        const uint64_t lanes = slots * 256;
+        const bool small_grp = n_grp * 4 < lanes;
+        std::vector<uint32_t> fan_of(grp.size(), 0), lv_of(grp.size(), 0);
+        bool any_split = false;
+        uint64_t items = 0;
+        {
+            const double share = 16.0 * std::max(64.0, est / (double)lanes);
+            for (size_t k = 0; k < grp.size(); k++) {
+                const Inst &in = inst_[grp[k]];
+                uint32_t f = 0;
                 for (int c = 0; c < kMaxWidth; c++)
-                    fan = std::max<uint32_t>(fan, inst_[id].desc.col_len[c]);
-        if (fan <= 1)
-            fan = 0;
-        const bool fan2 = fan && opts_.max_split_levels >= 2 &&
-                          n_grp * fan * 4 < slots * 256 && n_cur_ < slots * 256 * 16;
-        const uint64_t per = fan ? (fan2 ? (uint64_t)fan * fan : fan) : 1;
-        const uint64_t items = n_grp * per;
+                    f = std::max<uint32_t>(f, in.desc.col_len[c]);
+                uint32_t lv = 0;
+                if (f > 1) {
+                    if (small_grp)
+                        lv = n_grp * f * 4 < lanes && n_cur_ < lanes * 16 ? 2 : 1;
+                    else if (in.row == 0 || in.growth > share)
+                        lv = in.row > 0 && in.growth / f > share ? 2 : 1;
+                }
+                lv = std::min(lv, opts_.max_split_levels);
+                fan_of[k] = lv ? f : 0;
+                lv_of[k] = lv;
+                any_split |= lv > 0;
+                const uint64_t per = lv == 2 ? (uint64_t)f * f : lv == 1 ? f : 1;
+                items += in.seg_len * per;
+            }
+        }
         // Launch plan: warps take chunks independently, about
         // `chunks_per_warp` chunks per resident warp, within [32, chunk_cap]
         // items; the grid is `ctas` CTAs per SM.
@@ -946,12 +968,19 @@ StepStats Engine::step_impl() {
             segs.clear();
             n_chunks = 0;
             uint64_t tb = 0;
+            uint64_t item_off = 0;
             for (size_t k = 0; k < grp.size(); k++) {
                 const uint32_t id = grp[k];
                 const Inst &in = inst_[id];
                 Seg s = seg_for(id, in.row);
-                s.begin = in.seg_begin * per;
+                const uint64_t f = fan_of[k];
+                const uint64_t per = lv_of[k] == 2 ? f * f : lv_of[k] == 1 ? f : 1;
+                s.rec = in.seg_begin;
+                s.begin = item_off;
                 s.len = in.seg_len * per;
+                s.fan = fan_of[k];
+                s.levels = lv_of[k];
+                item_off += s.len;
                 s.chunk_base = n_chunks;
                 s.tbase = tb;
                 s.tcap = region[k];
@@ -967,7 +996,7 @@ StepStats Engine::step_impl() {
             grid = (int)std::min<uint64_t>(n_chunks, (uint64_t)sms_ * (uint64_t)ctas);
             return tot;
         };
-        if (opts_.autotune && !tune_.set && !fan && n_grp >= kTuneMinStates &&
+        if (opts_.autotune && !tune_.set && !any_split && n_grp >= kTuneMinStates &&
             n_grp <= kTuneMaxStates)
             autotune(grp, est, occ, plan, segs, chunk, n_chunks, grid);
         const uint64_t cap = plan(tune_);
@@ -1017,8 +1046,6 @@ StepStats Engine::step_impl() {
             a.n_segs = (uint32_t)segs.size();
             a.n_chunks = n_chunks;
             a.chunk_states = chunk;
-            a.fan = fan;
-            a.fan2 = fan2;
             a.insts = insts_.p;
             a.plc = plc_.p;
             a.filt = filt_.p;
@@ -1131,8 +1158,6 @@ StepStats Engine::step_impl() {
         a.n_segs = (uint32_t)segs.size();
         a.n_chunks = n_chunks;
         a.chunk_states = chunk;
-        a.fan = fan;
-        a.fan2 = fan2;
         a.insts = insts_.p;
         a.plc = plc_.p;
         a.filt = filt_.p;
@@ -1716,7 +1741,6 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
         a.n_segs = (uint32_t)segs.size();
         a.n_chunks = n_chunks;
         a.chunk_states = chunk;
-        a.fan = 0;
         a.insts = insts_.p;
         a.plc = plc_.p;
         a.filt = filt_.p;

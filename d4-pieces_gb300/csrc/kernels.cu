@@ -422,8 +422,6 @@ k_expand(ExpandArgs a) {
     }
     WarpStage &ws = stage[threadIdx.x >> 5];
     const unsigned lt_mask = (1u << lane) - 1u;
-    const uint32_t fan = a.fan ? a.fan : 1u;
-    const uint32_t per = a.fan2 ? fan * fan : fan;   // work items per state
     unsigned long long raw = 0;
 
     // Warp-uniform chunk cursor.
@@ -501,7 +499,14 @@ k_expand(ExpandArgs a) {
                 dyn_bits = d->dyn_bits;
                 dynmask = (1ull << dyn_bits) - 1ull;
                 usedmask = (1ull << d->used_bits) - 1ull;
-                const unsigned long long si = item / per;
+                // The item's state, and (a split segment) which first
+                // placements it fixes: item - begin = (state * fan + second)
+                // * fan + first.
+                const uint32_t lvs = sg->levels;
+                const uint32_t fs = lvs ? sg->fan : 1u;
+                const uint32_t per = lvs == 2 ? fs * fs : fs;
+                const unsigned long long rel = item - sg->begin;
+                const unsigned long long si = sg->rec + (lvs ? rel / per : rel);
                 const ulonglong2 rec = a.recs[si];
                 wit = (d->flags & kInstWitness) != 0u;
                 if constexpr (K64) {
@@ -519,17 +524,17 @@ k_expand(ExpandArgs a) {
                 idx = 0;
                 min_depth = 0;
                 active = true;
-                if (a.fan) {
+                if (lvs) {
                     // Place this item's first choice (and, split two ways,
                     // its second) and walk only beneath them: min_depth =
                     // the placements fixed.  Items whose choices do not fit
                     // are empty; a row completed early is emitted by the one
                     // item whose remaining choices are 0.
-                    const uint32_t rem = (uint32_t)(item % per);
-                    uint32_t choice = rem % fan;
-                    uint32_t later = rem / fan;   // choices below the current level
+                    const uint32_t rem = (uint32_t)(rel % per);   // per <= 2^16
+                    uint32_t choice = rem % fs;
+                    uint32_t later = rem / fs;   // choices below the current level
                     active = true;
-                    for (uint32_t lv = 0; active && lv < (a.fan2 ? 2u : 1u); ++lv) {
+                    for (uint32_t lv = 0; active && lv < lvs; ++lv) {
                         const uint32_t row = (uint32_t)w & rowmask;
                         if (row == 0) {
                             active = choice == 0 && later == 0;

@@ -16,11 +16,7 @@ struct ExpandArgs {
     const Seg *segs;
     uint32_t n_segs;
     uint64_t n_chunks;
-    uint64_t chunk_states;           // work items per chunk
-    uint32_t fan;                    // >0: split each state's walk by its first placement
-                                     // (work item = state * fan + first choice)
-    uint32_t fan2;                   // with fan: split by the first two placements
-                                     // (item = (state * fan + second) * fan + first)
+    uint64_t chunk_states;           // work items per chunk (a segment's split: Seg::levels)
     const InstDesc *insts;
     const Plc *plc;
     const unsigned long long *filt;  // candidate filter bitsets (InstDesc::filt_off)

@@ -239,9 +239,12 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
             const uint64_t warps = slots * 8;
             uint64_t chunk = (items + 8 * warps - 1) / (8 * warps);
             chunk = std::min<uint64_t>(std::max<uint64_t>((chunk + 31) / 32 * 32, 32), 1024);
+            sg.rec = 0;
             sg.begin = 0;
             sg.len = items;
             sg.chunk_base = 0;
+            sg.fan = fan;
+            sg.levels = fan ? (fan2 ? 2u : 1u) : 0u;
             const uint64_t n_chunks = (items + chunk - 1) / chunk;
             cuda_check(cudaMemcpyAsync(d_seg, &sg, sizeof(sg), cudaMemcpyHostToDevice, s),
                        "upload");
@@ -252,8 +255,6 @@ extern "C" int d4e_count_noalloc(const d4e_instance *inst, void *stream, uint64_
             a.n_segs = 1;
             a.n_chunks = n_chunks;
             a.chunk_states = chunk;
-            a.fan = fan;
-            a.fan2 = fan2;
             a.insts = d_desc;
             a.plc = d_plc;
             a.filt = d_filt;
