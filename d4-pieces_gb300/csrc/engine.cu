@@ -886,6 +886,10 @@ StepStats Engine::step_impl() {
         // fan = the instance's longest placement list of a column.
         const uint64_t lanes = slots * 256;
         const bool small_grp = n_grp * 4 < lanes;
+        static const bool split_heavy = [] {   // D4E_SPLIT_HEAVY=0: the group rule only
+            const char *v = std::getenv("D4E_SPLIT_HEAVY");
+            return !(v && std::strcmp(v, "0") == 0);
+        }();
         std::vector<uint32_t> fan_of(grp.size(), 0), lv_of(grp.size(), 0);
         bool any_split = false;
         uint64_t items = 0;
@@ -900,7 +904,7 @@ StepStats Engine::step_impl() {
                 if (f > 1) {
                     if (small_grp)
                         lv = n_grp * f * 4 < lanes && n_cur_ < lanes * 16 ? 2 : 1;
-                    else if (in.row == 0 || in.growth > share)
+                    else if (split_heavy && (in.row == 0 || in.growth > share))
                         lv = in.row > 0 && in.growth / f > share ? 2 : 1;
                 }
                 lv = std::min(lv, opts_.max_split_levels);
