@@ -311,6 +311,7 @@ Engine::~Engine() {
             cudaEventDestroy(e);
     plc_.release();
     filt_.release();
+    part_ctr_.release();
     insts_.release();
     inst_unique_.release();
     cursor_.release();
@@ -1178,6 +1179,24 @@ StepStats Engine::step_impl() {
         a.stage_plc = stage_plc(segs);
         a.u32 = counters_fit_u32(segs) ? 1u : 0u;
         a.single_word = multi_word_filters(segs) ? 0u : 1u;
+        // Multi-instance rows of an engine that is never preempted claim
+        // chunks by SM partition (ExpandArgs::parts; D4E_CLAIM_PARTS=0: one
+        // global counter).
+        {
+            static const bool parts_on = [] {
+                const char *v = std::getenv("D4E_CLAIM_PARTS");
+                return !(v && std::strcmp(v, "0") == 0);
+            }();
+            if (parts_on && k64_ && segs.size() > 1 && !opts_.preempt_flag) {
+                part_ctr_.reserve(sms_, stream_);
+                cuda_check(cudaMemsetAsync(part_ctr_.p, 0, sms_ * sizeof(unsigned long long),
+                                           stream_),
+                           "memset");
+                a.parts = (uint32_t)sms_;
+                a.part_step = (n_chunks + (uint64_t)sms_ - 1) / (uint64_t)sms_;
+                a.part_ctr = part_ctr_.p;
+            }
+        }
         // A launch that honours the preemption flag may end with chunks not
         // yet taken (the work counter below n_chunks): launch again, with
         // the counters kept, until the row is done.

@@ -370,6 +370,7 @@ private:
     DevBuf<Plc> plc_;
     uint64_t plc_total_ = 0, plc_uploaded_ = 0;
     DevBuf<unsigned long long> filt_;
+    DevBuf<unsigned long long> part_ctr_;   // k_expand partition counters (ExpandArgs::parts)
     uint64_t filt_total_ = 0, filt_uploaded_ = 0;
     DevBuf<InstDesc> insts_;
     DevBuf<unsigned int> inst_unique_;

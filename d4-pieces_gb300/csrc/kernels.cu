@@ -394,12 +394,20 @@ __device__ __forceinline__ uint32_t flush_children(const ExpandArgs &a, const Wa
 // while some lanes finish earlier items.
 // Completed rows are staged in shared memory and inserted by the whole
 // warp, 32 at a time.
-template <bool K64, bool U32, bool MW>
+template <bool K64, bool U32, bool MW, bool PARTS>
 __global__ void __launch_bounds__(kExpandBlock, 4)
 k_expand(ExpandArgs a) {
     using UT = std::conditional_t<U32, uint32_t, unsigned long long>;
     __shared__ WarpStage stage[kWarps];
     const unsigned lane = threadIdx.x & 31u;
+    // Partition claims: where each warp last found work (kept in shared
+    // memory, off the walk's registers).
+    __shared__ uint32_t s_part[kWarps];
+    if (PARTS && lane == 0) {
+        uint32_t smid;
+        asm("mov.u32 %0, %%smid;" : "=r"(smid));
+        s_part[threadIdx.x >> 5] = smid % a.parts;
+    }
     // Single-instance launch: the instance's descriptor and placement table
     // staged in shared memory (dynamic), read there by every walk step.
     const InstDesc *st_d = nullptr;
@@ -450,8 +458,32 @@ k_expand(ExpandArgs a) {
         while (need && !no_more) {
             if (c_next >= c_end) {
                 unsigned long long ci = ~0ull;
-                if (lane == 0 && !(a.preempt && *(const volatile unsigned int *)a.preempt))
-                    ci = atomicAdd(a.work, 1ull);
+                if (lane == 0) {
+                    if constexpr (PARTS) {
+                        // Own partition first, then the following ones; a
+                        // claim past a partition's end takes nothing.
+                        const uint32_t cur_part = s_part[threadIdx.x >> 5];
+                        for (uint32_t t = 0; t < a.parts; ++t) {
+                            const uint32_t q = cur_part + t < a.parts ? cur_part + t
+                                                                      : cur_part + t - a.parts;
+                            const unsigned long long lo0 = a.part_step * q;
+                            const unsigned long long lo = lo0 < a.n_chunks ? lo0 : a.n_chunks;
+                            const unsigned long long hi0 = lo + a.part_step;
+                            const unsigned long long hi = hi0 < a.n_chunks ? hi0 : a.n_chunks;
+                            if (lo >= hi)
+                                continue;
+                            const unsigned long long o = atomicAdd(a.part_ctr + q, 1ull);
+                            if (lo + o < hi) {
+                                ci = lo + o;
+                                s_part[threadIdx.x >> 5] = q;
+                                break;
+                            }
+                        }
+                    } else {
+                        if (!(a.preempt && *(const volatile unsigned int *)a.preempt))
+                            ci = atomicAdd(a.work, 1ull);
+                    }
+                }
                 ci = __shfl_sync(0xffffffffu, ci, 0);
                 if (ci >= a.n_chunks) {
                     no_more = true;
@@ -1548,26 +1580,36 @@ __global__ void k_count_pattern(const ulonglong2 *__restrict__ recs, unsigned lo
 }  // namespace
 
 cudaError_t expand_max_blocks_per_sm(bool k64, int *n) {
-    return k64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, k_expand<true, false, true>,
-                                                                kExpandBlock, 0)
-               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, k_expand<false, false, true>,
-                                                                kExpandBlock, 0);
+    return k64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                     n, k_expand<true, false, true, false>, kExpandBlock, 0)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                     n, k_expand<false, false, true, false>, kExpandBlock, 0);
 }
 
 void launch_expand(bool k64, const ExpandArgs &a, int grid, cudaStream_t s) {
     if (a.n_chunks == 0)
         return;
     const size_t dyn = a.stage_plc ? expand_stage_bytes(a.stage_plc) : 0;
-    if (k64)
+    // Partition claims (multi-instance packed-key launches) are a separate
+    // instantiation, so that the other launches keep the plain claim's
+    // registers.
+    if (k64 && a.parts)
         if (a.u32)
-            a.single_word ? k_expand<true, true, false><<<grid, kExpandBlock, dyn, s>>>(a)
-                          : k_expand<true, true, true><<<grid, kExpandBlock, dyn, s>>>(a);
+            a.single_word ? k_expand<true, true, false, true><<<grid, kExpandBlock, dyn, s>>>(a)
+                          : k_expand<true, true, true, true><<<grid, kExpandBlock, dyn, s>>>(a);
         else
-            a.single_word ? k_expand<true, false, false><<<grid, kExpandBlock, dyn, s>>>(a)
-                          : k_expand<true, false, true><<<grid, kExpandBlock, dyn, s>>>(a);
+            a.single_word ? k_expand<true, false, false, true><<<grid, kExpandBlock, dyn, s>>>(a)
+                          : k_expand<true, false, true, true><<<grid, kExpandBlock, dyn, s>>>(a);
+    else if (k64)
+        if (a.u32)
+            a.single_word ? k_expand<true, true, false, false><<<grid, kExpandBlock, dyn, s>>>(a)
+                          : k_expand<true, true, true, false><<<grid, kExpandBlock, dyn, s>>>(a);
+        else
+            a.single_word ? k_expand<true, false, false, false><<<grid, kExpandBlock, dyn, s>>>(a)
+                          : k_expand<true, false, true, false><<<grid, kExpandBlock, dyn, s>>>(a);
     else
-        a.single_word ? k_expand<false, false, false><<<grid, kExpandBlock, dyn, s>>>(a)
-                      : k_expand<false, false, true><<<grid, kExpandBlock, dyn, s>>>(a);
+        a.single_word ? k_expand<false, false, false, false><<<grid, kExpandBlock, dyn, s>>>(a)
+                      : k_expand<false, false, true, false><<<grid, kExpandBlock, dyn, s>>>(a);
 }
 
 namespace {

@@ -28,6 +28,14 @@ struct ExpandArgs {
     unsigned long long *n_raw;       // children produced (all instances)
     unsigned int *status;
     unsigned long long *work;        // dynamic chunk counter, zeroed before the row's first launch
+    // parts > 0 (launches that are never preempted): the chunk range is cut
+    // into `parts` contiguous partitions, each with its own counter in
+    // part_ctr (zeroed before the launch); a warp claims from its SM's
+    // partition first and from the next ones when it runs dry, so that an
+    // SM's warps walk few instances at a time.
+    uint32_t parts;
+    unsigned long long part_step;    // chunks per partition (the last one may hold fewer)
+    unsigned long long *part_ctr;
     // Cooperative preemption (nullptr = none): while *preempt is nonzero
     // (host memory mapped into the device), warps take no new chunk, finish
     // the items they hold and exit.  The launch then ends with *work <
