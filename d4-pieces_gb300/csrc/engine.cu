@@ -1849,7 +1849,7 @@ void Engine::autotune(const std::vector<uint32_t> &grp, double est, int occ,
         t.load = load;
         consider(t);
     }
-    // The dedup tile plan (k_compact blocks per SM x ring depth), judged on
+    // The dedup tile plan (k_compact blocks per SM x ring depth), chosen by
     // the compaction's own time, a few percent of the trial's.
     {
         trial(best);
